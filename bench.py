@@ -1,0 +1,320 @@
+"""Benchmark of the PERKS stencil time loop on GB300.
+
+Headline workload (the reference's stencil sweep, 2D star 9-point):
+2ds9pt, FP32 storage and arithmetic, 8192 x 8192 cells, 1000 time steps per
+step of this benchmark, persistent kernel with shared-memory-resident rows,
+reference evaluation order (bit-identical to the reference's CPU gold code).
+Input: seeded uniform [0,1) field (synthetic; the reference has no dataset
+for the stencils). The field (256 MiB) is larger than L2 (129 MB).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One JSON line on rank 0. N > 1 runs one independent replica per GPU
+("replicas only": the reference runs on one GPU and the path has no exchange
+between GPUs); value = cells*time_steps of all ranks / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SHAPE = "2ds9pt"
+WY = WX = 8192
+TSTEPS = 1000
+DTYPE = "f32"
+METRIC = "GCells/s per stencil & CG time-to-1e-10 rel. residual; mixed vs FP64 on GB300"
+UNIT = "GCells/s"
+# DRAM bytes (read + write) per cell per time step of the persistent kernel,
+# from the ncu capture summarised in profiles/stencil2d_2ds9pt_f32_8192.md
+# (None until a capture exists).
+TRAFFIC_PER_CELL_STEP = None
+
+
+def measured_hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(x: float, ws: int, device=None) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device if device is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_baseline(seconds_budget: float = 15.0):
+    """The oracle (C restatement of the reference's CPU gold code, OpenMP over
+    rows) on this host's cores, on a bounded sample of the workload."""
+    import numpy as np
+    from oracle import oracle as O
+    O.build()
+    rng = np.random.default_rng(0)
+    f = rng.random((WY, WX), dtype=np.float32)
+    steps = 1
+    t0 = time.perf_counter()
+    O.stencil(SHAPE, f, steps)
+    dt = time.perf_counter() - t0
+    steps = max(1, min(50, int(seconds_budget / max(dt, 1e-3))))
+    t0 = time.perf_counter()
+    O.stencil(SHAPE, f, steps)
+    dt = time.perf_counter() - t0
+    return {"value": WY * WX * steps / dt / 1e9, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+            "sample": f"{SHAPE} fp32 {WY}x{WX}, {steps} time steps (of {TSTEPS}), oracle C port, OpenMP"}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    K, W = args.steps, args.warmup
+    for _ in range(W):
+        cpu_baseline(seconds_budget=2.0)
+    vals = []
+    t0 = time.perf_counter()
+    last = None
+    for _ in range(K):
+        last = cpu_baseline(seconds_budget=max(2.0, 60.0 / max(K, 1)))
+        vals.append(last["value"])
+    el = time.perf_counter() - t0
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": K,
+            "warmup": W, "ms_per_step": el * 1e3 / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": DTYPE, "data": "synthetic",
+            "config": {"workload": f"{SHAPE} {DTYPE} {WY}x{WX} x{TSTEPS} time steps", "shape": SHAPE,
+                       "cells": WY * WX, "time_steps": TSTEPS},
+            "cpu_baseline": {**last, "value": v},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extra", action="store_true", help="skip the comparator measurements")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend=backend)
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    import numpy as np
+    import torch
+
+    import perks_gb300 as P
+    from perks_gb300 import _native as N
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    P.lib()
+    stream = torch.cuda.current_stream(dev)
+    g = torch.Generator(device="cpu").manual_seed(1234 + rank)
+    host = torch.rand((WY, WX), generator=g, dtype=torch.float32).pin_memory()
+    hout = torch.empty_like(host).pin_memory()
+    d_in = host.to(dev)
+    d_out = torch.empty_like(d_in)
+    kw = dict(kernel="persistent", order="reference", l2_sweep=False)
+
+    def step():
+        _, st = P.stencil2d(d_in, SHAPE, TSTEPS, out=d_out, **kw)
+        return st
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    P.reset_launch_count()
+    kernel_ms = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        barrier(ws)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            st = step()
+            kernel_ms.append(st["ms"])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(ws)
+    launches = P.launch_count()
+    ms = e0.elapsed_time(e1)
+    ms_max = max_over_ranks(ms, ws, dev if ws > 1 else None)
+    cells = WY * WX * TSTEPS
+    value = cells * args.steps * ws / (ms_max * 1e-3) / 1e9
+
+    # e2e: the reference-facing host-buffer entry point (jacobi_iterative),
+    # pinned host buffers, H2D + D2H inside the timed region.
+    lib = P.lib()
+    hin_p = ctypes.c_void_p(host.data_ptr())
+    hout_p = ctypes.c_void_p(hout.data_ptr())
+
+    def e2e_step():
+        rc = lib.perks_jacobi_iterative_f32(N.SHAPES[SHAPE], hin_p, WY, WX, hout_p, 256, 0, TSTEPS, 0, 1, 0, -1, 0)
+        if rc != 0:
+            raise RuntimeError(P.last_error())
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, ws, dev if ws > 1 else None)
+    barrier(ws)
+    e2e_val = cells * args.steps * ws / e2e_s / 1e9
+    nbytes = WY * WX * 4
+
+    peak, peak_src = measured_hbm_peak()
+    kms = statistics.mean(kernel_ms)
+    alg_bytes = 2 * 4 * cells  # reference formula: 2*sizeof(REAL)*cells per time step
+    achieved = alg_bytes / (kms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_source": peak_src,
+            "traffic": (TRAFFIC_PER_CELL_STEP * cells) if TRAFFIC_PER_CELL_STEP else None,
+            "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms_per_launch": round(kms, 3)}
+
+    extra = {}
+    if not args.no_extra and rank == 0:
+        # one-launch-per-step comparator and FP64 on the same shape and size
+        _, st = P.stencil2d(d_in, SHAPE, 100, out=d_out, kernel="per_step")
+        extra["per_step_fp32_gcells"] = round(st["gcells_per_s"], 2)
+        _, st = P.stencil2d(d_in, SHAPE, 100, out=d_out, kernel="persistent", l2_sweep=True)
+        extra["persistent_l2sweep_fp32_gcells"] = round(st["gcells_per_s"], 2)
+        _, st = P.stencil2d(d_in, SHAPE, 100, out=d_out, kernel="persistent", order="fast")
+        extra["persistent_fast_fp32_gcells"] = round(st["gcells_per_s"], 2)
+        d64 = d_in.double()
+        o64 = torch.empty_like(d64)
+        _, st = P.stencil2d(d64, SHAPE, 50, out=o64, kernel="persistent")
+        extra["persistent_ref_fp64_gcells"] = round(st["gcells_per_s"], 2)
+        _, st = P.stencil2d(d64, SHAPE, 50, out=o64, kernel="persistent", order="fast")
+        extra["persistent_fast_fp64_gcells"] = round(st["gcells_per_s"], 2)
+        del d64, o64
+        extra["cached_fraction"] = round(kernel_cached_fraction(P, d_in, d_out), 4)
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_baseline()
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": max(3, args.warmup), "ms_per_step": round(ms_max / args.steps, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPE,
+                "data": "synthetic (seeded uniform [0,1) field)",
+                "config": {"workload": f"{SHAPE} {DTYPE} {WY}x{WX} x{TSTEPS} time steps, persistent, "
+                                       f"reference order", "shape": SHAPE, "cells": WY * WX,
+                           "time_steps_per_step": TSTEPS, "parallelism": f"replicas{ws}",
+                           "l2": "inputs larger than L2 (256 MiB field)"},
+                "e2e": {"value": round(e2e_val, 3), "unit": UNIT, "h2d_bytes_per_step": nbytes,
+                        "d2h_bytes_per_step": nbytes},
+                "gpu_launches": int(launches),
+                "roofline": roof,
+                "cpu_baseline": cpu,
+                "clocks": clk.summary(),
+                "extra": extra}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def kernel_cached_fraction(P, d_in, d_out):
+    _, st = P.stencil2d(d_in, SHAPE, 2, out=d_out)
+    return st["cached_fraction"]
+
+
+if __name__ == "__main__":
+    main()

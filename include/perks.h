@@ -1,0 +1,212 @@
+/*
+ * perks.h — C ABI of the GB300 (sm_103a) PERKS stencil and CG library.
+ *
+ * Plain C types only: device or host pointers, sizes, small option structs.
+ * Every entry point returns a status code and never exits the process; a
+ * human-readable message for the last failure on the calling thread is
+ * available from perks_last_error().
+ *
+ * Each entry point names the reference interface it replaces (paths inside
+ * the neozhang307/PERKS project).
+ */
+#ifndef PERKS_GB300_H
+#define PERKS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define PERKS_API __attribute__((visibility("default")))
+#else
+#define PERKS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PERKS_ABI_VERSION 1
+
+/* ------------------------------------------------------------------ codes */
+typedef enum {
+  PERKS_OK = 0,
+  PERKS_ERR_INVALID_ARG = -10,  /* null pointer, bad size, unknown enum */
+  PERKS_ERR_UNSUPPORTED = -11,  /* shape/dtype/size combination not built */
+  PERKS_ERR_NO_DEVICE = -12,    /* no CUDA device / driver */
+  PERKS_ERR_CUDA = -13,         /* a CUDA runtime call failed */
+  PERKS_ERR_OOM = -14,          /* device allocation failed */
+  PERKS_ERR_TIMEOUT = -15,      /* a device-side wait ran out its budget */
+  PERKS_ERR_LAUNCH = -16,       /* cooperative grid does not fit the GPU */
+  PERKS_ERR_BREAKDOWN = -17,    /* CG: p.Ap <= 0 or non-finite (matrix not SPD) */
+  PERKS_ERR_NOT_CONVERGED = -18 /* CG: max_iter reached before the tolerance */
+} perks_status;
+
+/* Stencil shapes, one per reference executable
+ * (stencil/2dstencil/<shape>/, stencil/3dstencil/<shape>/). */
+typedef enum {
+  PERKS_2D5PT = 0,   /* star, halo 1 */
+  PERKS_2DS9PT = 1,  /* star, halo 2 */
+  PERKS_2D13PT = 2,  /* star, halo 3 */
+  PERKS_2D17PT = 3,  /* star, halo 4 */
+  PERKS_2D21PT = 4,  /* star, halo 5 */
+  PERKS_2DS25PT = 5, /* star, halo 6 */
+  PERKS_2D9PT = 6,   /* box 3x3 */
+  PERKS_2D25PT = 7,  /* box 5x5 */
+  PERKS_3D7PT = 16,  /* star, halo 1 */
+  PERKS_3D13PT = 17, /* star, halo 2 */
+  PERKS_3D17PT = 18, /* corners + centre plane, halo 1 */
+  PERKS_3D27PT = 19, /* box 3x3x3 */
+  PERKS_POISSON = 20 /* 19-point, halo 1 */
+} perks_shape;
+
+typedef enum { PERKS_FP32 = 0, PERKS_FP64 = 1, PERKS_MIXED = 2 } perks_dtype;
+
+typedef enum {
+  PERKS_BOUNDARY_CLAMP = 0,    /* reference semantics: out-of-range neighbours clamp to the edge */
+  PERKS_BOUNDARY_DIRICHLET = 1 /* the outer `halo` cells on each face stay fixed */
+} perks_boundary;
+
+typedef enum {
+  PERKS_ORDER_REFERENCE = 0, /* bit-identical to the reference CPU gold code */
+  PERKS_ORDER_FAST = 1       /* folded coefficients + FMA */
+} perks_order;
+
+typedef enum {
+  PERKS_KERNEL_PERSISTENT = 0, /* one cooperative launch for all steps, rows/planes kept on chip */
+  PERKS_KERNEL_PER_STEP = 1    /* one launch per time step, nothing kept on chip (comparator) */
+} perks_kernel;
+
+/* --------------------------------------------------------------- stencils */
+typedef struct {
+  int shape;       /* perks_shape */
+  int dtype;       /* PERKS_FP32 or PERKS_FP64 (storage and arithmetic type) */
+  int boundary;    /* perks_boundary */
+  int order;       /* perks_order */
+  int kernel;      /* perks_kernel */
+  int cache_rows;  /* persistent kernel: rows (2D) / planes (3D) per CTA kept in shared memory;
+                      -1 = as many as fit, 0 = none */
+  int l2_sweep;    /* persistent kernel: alternate the sweep direction each step and drop dead
+                      lines from L2, so the rows written last are read first from L2 (1 = on) */
+  int tile_x;      /* columns per CTA tile; 0 = auto */
+  int tile_y;      /* 3D only: rows per CTA tile; 0 = auto */
+  int ctas;        /* CTAs in the persistent grid; 0 = one per SM */
+  void* stream;    /* cudaStream_t; NULL = legacy default stream */
+} perks_stencil_opts;
+
+typedef struct {
+  double ms;            /* device time of the stencil kernels (CUDA events), excludes layout copies */
+  double gcells_per_s;  /* cells * steps / ms / 1e6 (reference formula, jacobi-2d.cu:822) */
+  double cached_fraction; /* share of cells kept in shared memory across steps */
+  int grid_x, grid_y, grid_z; /* tile grid */
+  int tile_x, tile_y;
+  int cached_rows;      /* rows (2D) / planes (3D) per CTA kept in shared memory */
+  int launches;         /* kernels launched by the call */
+} perks_stencil_stats;
+
+/* Fill `opts` with defaults for a shape and dtype. */
+PERKS_API void perks_stencil_default_opts(perks_stencil_opts* opts, int shape, int dtype);
+
+/* 2D Jacobi time loop on device buffers.
+ * d_in: width_y*width_x row-major, not modified. d_out: same size, written.
+ * d_in and d_out must not overlap. `steps` >= 0 (0 copies d_in to d_out).
+ * Replaces the device path of jacobi_iterative<REAL>
+ * (stencil/2dstencil/jacobi-2d.cu:371-865). `stats` may be NULL. */
+PERKS_API int perks_stencil2d(const perks_stencil_opts* opts, const void* d_in, void* d_out, int width_y,
+                    int width_x, int steps, perks_stencil_stats* stats);
+
+/* 3D Jacobi time loop on device buffers, layout [height][width_y][width_x].
+ * Replaces the device path of j3d_iterative<REAL>
+ * (stencil/3dstencil/j3d.cu:129-808). */
+PERKS_API int perks_stencil3d(const perks_stencil_opts* opts, const void* d_in, void* d_out, int height,
+                    int width_y, int width_x, int steps, perks_stencil_stats* stats);
+
+/* Host-buffer drop-ins with the reference's argument list. The stencil shape
+ * is the first argument (the reference fixes it per executable with -D
+ * macros). bdimx/blkpsm/async/useSM/isDoubleTile keep their meaning where
+ * it carries over: useSM=0 disables shared-memory row caching; the others are
+ * accepted and ignored. usewarmup runs `warmupiteration` (or `iteration`
+ * when <=0) untimed steps first. Returns 0 on success, the reference's code 1
+ * (jacobi-2d.cu:600) never, and a negative perks_status on failure.
+ * Replaces jacobi_iterative<float/double> (stencil/2dstencil/common/jacobi_cuda.cuh:6-10). */
+PERKS_API int perks_jacobi_iterative_f32(int shape, const float* h_in, int width_y, int width_x, float* h_out,
+                               int bdimx, int blkpsm, int iteration, int async, int useSM,
+                               int usewarmup, int warmupiteration, int isDoubleTile);
+PERKS_API int perks_jacobi_iterative_f64(int shape, const double* h_in, int width_y, int width_x,
+                               double* h_out, int bdimx, int blkpsm, int iteration, int async,
+                               int useSM, int usewarmup, int warmupiteration, int isDoubleTile);
+/* Replaces j3d_iterative<float/double> (stencil/3dstencil/common/jacobi_cuda.cuh:6-10).
+ * Reference return codes kept: -2 unsupported widths, -4 height too small. */
+PERKS_API int perks_j3d_iterative_f32(int shape, const float* h_in, int height, int width_y, int width_x,
+                            float* h_out, int bdimx, int blkpsm, int iteration, int useSM,
+                            int usewarmup, int warmupiteration, int isDoubleTile, int getminHeight);
+PERKS_API int perks_j3d_iterative_f64(int shape, const double* h_in, int height, int width_y, int width_x,
+                            double* h_out, int bdimx, int blkpsm, int iteration, int useSM,
+                            int usewarmup, int warmupiteration, int isDoubleTile, int getminHeight);
+
+/* --------------------------------------------------------------------- CG */
+typedef enum {
+  PERKS_STOP_ABS_RR = 0, /* reference: stop when r.r < tol*tol (cg_kernels.cuh:834) */
+  PERKS_STOP_REL = 1     /* stop when ||r|| / ||b|| < tol */
+} perks_cg_stop;
+
+typedef struct {
+  int dtype;          /* PERKS_FP64, PERKS_FP32 (reference float build), PERKS_MIXED
+                         (FP32 inner CG, FP64 x, true residual and refinement) */
+  int stop;           /* perks_cg_stop */
+  double tol;
+  int max_iter;       /* iteration cap (inner iterations for PERKS_MIXED) */
+  int static_iter;    /* 1 = run exactly max_iter iterations (reference --staticiter) */
+  int kernel;         /* PERKS_KERNEL_PERSISTENT (one cooperative launch) or PERKS_KERNEL_PER_STEP */
+  int replace_every;  /* PERKS_MIXED: recompute r = b - A x in FP64 every this many inner iterations
+                         (0 = auto) */
+  int ctas;           /* CTAs in the persistent grid; 0 = auto */
+  void* stream;       /* cudaStream_t */
+} perks_cg_opts;
+
+typedef struct {
+  int iterations;        /* CG iterations executed (inner iterations summed for PERKS_MIXED) */
+  int outer;             /* PERKS_MIXED: residual replacements / refinement restarts */
+  double rr;             /* last recursive r.r */
+  double true_rel_res;   /* ||b - A x|| / ||b|| recomputed in FP64 on the device after the solve */
+  double ms;             /* device time of the solve */
+  int launches;
+} perks_cg_result;
+
+PERKS_API void perks_cg_default_opts(perks_cg_opts* opts);
+
+/* Solve A x = b with CG. A in CSR (int32 row_ptr[n+1], col[nnz]; values FP64
+ * for PERKS_FP64/PERKS_MIXED, FP32 for PERKS_FP32). x holds the initial guess
+ * on entry and the solution on return (FP64 except for PERKS_FP32). All
+ * pointers are device pointers. Replaces DispatchCG::ProcessDispatchCG
+ * (conjugateGradient/cg_dispatcher.cuh:559-916) and the kernel
+ * gpuConjugateGradient_cub (conjugateGradient/cg_kernels.cuh:620-986). */
+PERKS_API int perks_cg_csr(int n, int nnz, const int* d_row_ptr, const int* d_col, const void* d_val,
+                 const void* d_b, void* d_x, const perks_cg_opts* opts, perks_cg_result* res);
+
+/* CG with A in DIA format: `ndiag` diagonals with offsets h_offsets[ndiag]
+ * (host array, |offset| < n, at most 32 diagonals), values d_data[ndiag][n]
+ * diagonal-major where d_data[k*n + i] = A[i][i + offset[k]] (zero where
+ * i + offset is out of range). Generalises the reference's tridiagonal DIA
+ * SpMV (conjugateGradient/cg_dia_kernels.cuh:184-231) to k diagonals. */
+PERKS_API int perks_cg_dia(int n, int ndiag, const int* h_offsets, const void* d_data, const void* d_b,
+                 void* d_x, const perks_cg_opts* opts, perks_cg_result* res);
+
+/* y = A x for CSR / DIA (dtype PERKS_FP32 or PERKS_FP64). Building blocks
+ * exposed for tests and callers that run their own iteration. */
+PERKS_API int perks_spmv_csr(int dtype, int n, int nnz, const int* d_row_ptr, const int* d_col,
+                   const void* d_val, const void* d_x, void* d_y, void* stream);
+PERKS_API int perks_spmv_dia(int dtype, int n, int ndiag, const int* h_offsets, const void* d_data,
+                   const void* d_x, void* d_y, void* stream);
+
+/* ------------------------------------------------------------------ misc */
+PERKS_API const char* perks_last_error(void);     /* thread-local message of the last failure */
+PERKS_API const char* perks_status_string(int status);
+PERKS_API int perks_abi_version(void);
+/* Kernels launched by this thread since the counter was last reset. */
+PERKS_API long long perks_launch_count(void);
+PERKS_API void perks_reset_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PERKS_GB300_H */

@@ -1,0 +1,178 @@
+// Thin inline-PTX helpers for sm_103a: mbarriers, bulk (TMA) copies, proxy
+// fences, L2 cache policies, and a bounded grid barrier.
+//
+// Every wait in this file is bounded by a clock64() budget. When a budget
+// runs out the caller gets `false`, records an error word in global memory and
+// leaves its kernel; nothing here traps or spins forever.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace perks {
+
+// Error bits written to the device-side status word.
+enum : unsigned {
+  kErrBarrierTimeout = 1u << 0,   // grid barrier budget exhausted
+  kErrCopyTimeout = 1u << 1,      // an mbarrier (bulk copy) wait ran out
+  kErrPeerAbort = 1u << 2,        // another CTA reported an error first
+  kErrBreakdown = 1u << 3,        // CG: p.Ap <= 0 or non-finite
+  kErrNonFinite = 1u << 4,        // CG: non-finite residual
+};
+
+// About 2^32 clocks (~2 s at 2 GHz): far above any legitimate wait.
+constexpr long long kWaitBudget = 1ll << 32;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// ---------------------------------------------------------------- mbarrier
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// Make mbarrier initialisation visible to the async proxy (bulk copies).
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for phase `parity` of `bar`. Returns false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > kWaitBudget) return false;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------- L2 policy
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_normal() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+// ------------------------------------------------------------- bulk copies
+// Global -> shared bulk copy completing on `bar` (tx-count). Both addresses
+// 16-byte aligned and `bytes` a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, unsigned bytes,
+                                         uint64_t* bar, uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], "
+      "%4;" ::"r"(smem_u32(dst_smem)),
+      "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
+}
+
+// ------------------------------------------------------------------ fences
+// Order this thread's generic-proxy global writes before later async-proxy
+// (bulk copy) reads of the same addresses, possibly by other CTAs.
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Drop one 128-byte L2 line without writing it back. Only for data that is
+// dead: nobody reads it again before it is overwritten.
+__device__ __forceinline__ void l2_discard_line(const void* gptr) {
+  asm volatile("discard.global.L2 [%0], 128;" ::"l"(gptr) : "memory");
+}
+
+// ------------------------------------------------------------ stores/loads
+template <class V>
+__device__ __forceinline__ void st_global_policy(V* p, const V& v, uint64_t pol);
+
+template <>
+__device__ __forceinline__ void st_global_policy<float4>(float4* p, const float4& v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.x), "f"(v.y),
+               "f"(v.z), "f"(v.w), "l"(pol)
+               : "memory");
+}
+template <>
+__device__ __forceinline__ void st_global_policy<double2>(double2* p, const double2& v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(p), "d"(v.x), "d"(v.y), "l"(pol)
+               : "memory");
+}
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// ------------------------------------------------------------- grid barrier
+// Sense-reversing barrier over all CTAs of a cooperative launch.
+// bar[0] = arrival count, bar[1] = generation. `status` is the kernel's error
+// word: a CTA that finds it non-zero leaves the barrier early so that one
+// failing CTA does not make every other CTA wait out its budget.
+// Returns false when the caller must abandon the kernel.
+struct GridBarrier {
+  unsigned* bar;
+  unsigned* status;
+  unsigned nblocks;
+
+  __device__ __forceinline__ bool sync() {
+    __shared__ unsigned s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned ok = 1;
+      unsigned gen = ld_acquire_gpu(bar + 1);
+      __threadfence();
+      unsigned arrived = atomicAdd(bar, 1u) + 1u;
+      if (arrived == nblocks) {
+        atomicExch(bar, 0u);
+        __threadfence();
+        st_release_gpu(bar + 1, gen + 1u);
+      } else {
+        long long t0 = clock64();
+        while (ld_acquire_gpu(bar + 1) == gen) {
+          if (*((volatile unsigned*)status) != 0u) { ok = 0; break; }
+          if (clock64() - t0 > kWaitBudget) {
+            atomicOr(status, kErrBarrierTimeout);
+            ok = 0;
+            break;
+          }
+        }
+      }
+      if (ok && *((volatile unsigned*)status) != 0u) ok = 0;
+      s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+  }
+};
+
+}  // namespace perks

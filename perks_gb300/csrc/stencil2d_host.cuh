@@ -1,0 +1,155 @@
+// Host launcher for the 2D stencil kernel: tile planning, shared-memory
+// budget for resident rows, layout copies, cooperative or per-step launch.
+#pragma once
+#include <algorithm>
+#include <string>
+#include "runtime.cuh"
+#include "stencil2d.cuh"
+
+namespace perks {
+
+constexpr int kNT2D = 256;
+
+inline int ceil_div(long long a, long long b) { return int((a + b - 1) / b); }
+
+template <class T, int SHAPE, bool FAST>
+int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int wy, int wx, int steps,
+                     perks_stencil_stats* st) {
+  using Cf = Cfg2D<T, SHAPE, kNT2D>;
+  constexpr int H = Cf::H, R = Cf::R;
+  const DeviceInfo* dev = device_info();
+  if (!dev) return PERKS_ERR_NO_DEVICE;
+  cudaStream_t s = static_cast<cudaStream_t>(o.stream);
+  const bool persistent = o.kernel == PERKS_KERNEL_PERSISTENT;
+  const int ctas = o.ctas > 0 ? std::min(o.ctas, dev->sms) : dev->sms;
+  const int gx = ceil_div(wx, Cf::TX);
+  if (gx > ctas)
+    return fail(PERKS_ERR_UNSUPPORTED, "width_x " + std::to_string(wx) + " needs more than " +
+                                           std::to_string(ctas) + " column tiles");
+  const int gy = std::max(1, std::min(ctas / gx, wy));
+  const int pitch = gx * Cf::TX;
+  const int tymax = ceil_div(wy, gy);
+
+  size_t fixed = Cf::ring_bytes + Cf::bar_bytes;
+  int C = 0, M = 0;
+  if (persistent && o.cache_rows != 0 && steps > 1) {
+    long long avail = (long long)dev->smem_optin - (long long)fixed - 256;
+    int cmax = int(avail / (long long)Cf::row_bytes) - (R + H);
+    if (o.cache_rows > 0) cmax = std::min(cmax, o.cache_rows);
+    C = std::min(cmax, tymax - 2 * H);
+    if (C <= 0) C = 0;
+    M = C > 0 ? C + R + H : 0;
+  }
+  const size_t smem = fixed + size_t(M) * Cf::row_bytes;
+  if (smem > dev->smem_optin) return fail(PERKS_ERR_UNSUPPORTED, "shared memory budget exceeded");
+
+  if (st) {
+    *st = perks_stencil_stats{};
+    st->grid_x = gx;
+    st->grid_y = gy;
+    st->grid_z = 1;
+    st->tile_x = Cf::TX;
+    st->tile_y = tymax;
+    st->cached_rows = C;
+  }
+  const size_t elems = size_t(wy) * wx;
+  if (steps == 0) {
+    PERKS_CUDA(cudaMemcpyAsync(d_out, d_in, elems * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    PERKS_CUDA(cudaStreamSynchronize(s));
+    return PERKS_OK;
+  }
+
+  int stt = PERKS_OK;
+  const size_t fbytes = size_t(wy) * pitch * sizeof(T);
+  T* f0 = static_cast<T*>(workspace(kWsField0, fbytes, &stt));
+  if (!f0) return stt;
+  T* f1 = static_cast<T*>(workspace(kWsField1, fbytes, &stt));
+  if (!f1) return stt;
+  SyncWords sw;
+  if ((stt = sync_words(&sw, s)) != PERKS_OK) return stt;
+
+  PERKS_CUDA(cudaMemcpy2DAsync(f0, size_t(pitch) * sizeof(T), d_in, size_t(wx) * sizeof(T), size_t(wx) * sizeof(T),
+                               wy, cudaMemcpyDeviceToDevice, s));
+
+  Stencil2DParams p{};
+  p.f[0] = f0;
+  p.f[1] = f1;
+  p.wy = wy;
+  p.wx = wx;
+  p.pitch = pitch;
+  p.gx = gx;
+  p.gy = gy;
+  p.C = C;
+  p.M = M;
+  p.dirichlet = o.boundary == PERKS_BOUNDARY_DIRICHLET;
+  p.alternate = persistent && o.l2_sweep;
+  p.persistent = persistent;
+  p.bar = sw.bar;
+  p.status = sw.status;
+
+  auto kern = stencil2d_kernel<T, SHAPE, FAST, kNT2D>;
+  PERKS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  const int grid = gx * gy;
+  cudaEvent_t e0, e1;
+  PERKS_CUDA(cudaEventCreate(&e0));
+  PERKS_CUDA(cudaEventCreate(&e1));
+  PERKS_CUDA(cudaEventRecord(e0, s));
+  int launches = 0;
+  if (persistent) {
+    int nb = 0;
+    PERKS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kNT2D, smem));
+    if (nb * dev->sms < grid) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return fail(PERKS_ERR_LAUNCH, "persistent grid of " + std::to_string(grid) + " CTAs does not fit (" +
+                                        std::to_string(nb) + " per SM)");
+    }
+    p.steps = steps;
+    p.t0 = 0;
+    void* args[] = {&p};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kNT2D), args, smem, s);
+    if (e != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return cuda_fail(e, "cudaLaunchCooperativeKernel(stencil2d)");
+    }
+    launches = 1;
+  } else {
+    p.steps = 1;
+    for (int t = 0; t < steps; t++) {
+      p.t0 = t;
+      kern<<<grid, kNT2D, smem, s>>>(p);
+    }
+    launches = steps;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return cuda_fail(e, "stencil2d per-step launch");
+    }
+  }
+  PERKS_CUDA(cudaEventRecord(e1, s));
+  count_launch(launches);
+  PERKS_CUDA(cudaMemcpy2DAsync(d_out, size_t(wx) * sizeof(T), (steps & 1) ? f1 : f0, size_t(pitch) * sizeof(T),
+                               size_t(wx) * sizeof(T), wy, cudaMemcpyDeviceToDevice, s));
+  int rc = check_status(sw, s);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != PERKS_OK) return rc;
+  if (st) {
+    st->ms = ms;
+    st->gcells_per_s = double(elems) * steps / (double(ms) * 1e6);
+    long long cached = 0;
+    for (int ti = 0; ti < gy; ti++) {
+      int r0 = int((long long)ti * wy / gy), r1 = int((long long)(ti + 1) * wy / gy);
+      cached += std::max(0, std::min(C, r1 - r0 - 2 * H));
+    }
+    st->cached_fraction = double(cached) / double(wy);
+    st->launches = launches;
+  }
+  return PERKS_OK;
+}
+
+}  // namespace perks

@@ -1,0 +1,112 @@
+"""Host-side mirror of the reference's stencil interface.
+
+* ``jacobi_iterative`` / ``j3d_iterative`` keep the argument list of the
+  reference's host API (stencil/2dstencil/common/jacobi_cuda.cuh:6-10,
+  stencil/3dstencil/common/jacobi_cuda.cuh:6-10) over host (numpy) arrays and
+  return its int status; the shape, fixed per executable in the reference by
+  -D macros, is a keyword argument.
+* ``stencil2d`` / ``stencil3d`` run on device tensors (torch is used only to
+  own device memory and streams) and return the output and launch stats.
+
+Every call goes through libperks_gb300.so; there is no other code path.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+
+
+def _opts(shape: str, dtype, order="reference", kernel="persistent", boundary="clamp", cache_rows=-1,
+          l2_sweep=False, ctas=0, stream=None) -> N.StencilOpts:
+    if shape not in N.SHAPES:
+        raise ValueError(f"unknown shape {shape!r}")
+    o = N.StencilOpts()
+    dt = N.FP64 if np.dtype(dtype) == np.float64 else N.FP32
+    N.lib().perks_stencil_default_opts(ctypes.byref(o), N.SHAPES[shape], dt)
+    o.order = {"reference": N.ORDER_REFERENCE, "fast": N.ORDER_FAST}[order]
+    o.kernel = {"persistent": N.KERNEL_PERSISTENT, "per_step": N.KERNEL_PER_STEP}[kernel]
+    o.boundary = {"clamp": N.CLAMP, "dirichlet": N.DIRICHLET}[boundary]
+    o.cache_rows = int(cache_rows)
+    o.l2_sweep = int(bool(l2_sweep))
+    o.ctas = int(ctas)
+    o.stream = stream
+    return o
+
+
+def _stats(st: N.StencilStats) -> dict:
+    return {k: getattr(st, k) for k, _ in N.StencilStats._fields_}
+
+
+def _torch_dtype_np(t):
+    import torch
+    if t.dtype == torch.float32:
+        return np.float32
+    if t.dtype == torch.float64:
+        return np.float64
+    raise TypeError("stencil fields must be float32 or float64")
+
+
+def stencil2d(field, shape: str, steps: int, out=None, **kw):
+    """`steps` Jacobi steps of a 2D shape on a CUDA tensor (wy, wx)."""
+    import torch
+    if field.dim() != 2 or not field.is_cuda:
+        raise ValueError("field must be a 2D CUDA tensor")
+    field = field.contiguous()
+    out = torch.empty_like(field) if out is None else out
+    if "stream" not in kw:
+        kw["stream"] = ctypes.c_void_p(torch.cuda.current_stream(field.device).cuda_stream)
+    o = _opts(shape, _torch_dtype_np(field), **kw)
+    st = N.StencilStats()
+    N.check(N.lib().perks_stencil2d(ctypes.byref(o), field.data_ptr(), out.data_ptr(), field.shape[0],
+                                    field.shape[1], int(steps), ctypes.byref(st)))
+    return out, _stats(st)
+
+
+def stencil3d(field, shape: str, steps: int, out=None, **kw):
+    """`steps` Jacobi steps of a 3D shape on a CUDA tensor (h, wy, wx)."""
+    import torch
+    if field.dim() != 3 or not field.is_cuda:
+        raise ValueError("field must be a 3D CUDA tensor")
+    field = field.contiguous()
+    out = torch.empty_like(field) if out is None else out
+    if "stream" not in kw:
+        kw["stream"] = ctypes.c_void_p(torch.cuda.current_stream(field.device).cuda_stream)
+    o = _opts(shape, _torch_dtype_np(field), **kw)
+    st = N.StencilStats()
+    N.check(N.lib().perks_stencil3d(ctypes.byref(o), field.data_ptr(), out.data_ptr(), field.shape[0],
+                                    field.shape[1], field.shape[2], int(steps), ctypes.byref(st)))
+    return out, _stats(st)
+
+
+def jacobi_iterative(h_input: np.ndarray, width_y: int, width_x: int, output: np.ndarray, bdimx: int = 256,
+                     blkpsm: int = 0, iteration: int = 3, async_: bool = False, useSM: bool = True,
+                     usewarmup: bool = False, warmupiteration: int = -1, isDoubleTile: bool = False, *,
+                     shape: str = "2d5pt") -> int:
+    """Reference host API (jacobi-2d.cu:371): host arrays in and out, int status."""
+    if h_input.dtype not in (np.float32, np.float64) or output.dtype != h_input.dtype:
+        raise TypeError("float32 or float64 arrays of one dtype")
+    if not (h_input.flags["C_CONTIGUOUS"] and output.flags["C_CONTIGUOUS"]):
+        raise ValueError("arrays must be C-contiguous")
+    fn = N.lib().perks_jacobi_iterative_f64 if h_input.dtype == np.float64 else N.lib().perks_jacobi_iterative_f32
+    return fn(N.SHAPES[shape], h_input.ctypes.data, width_y, width_x, output.ctypes.data, bdimx, blkpsm,
+              iteration, int(async_), int(useSM), int(usewarmup), warmupiteration, int(isDoubleTile))
+
+
+def j3d_iterative(h_input: np.ndarray, height: int, width_y: int, width_x: int, output: np.ndarray,
+                  bdimx: int = 256, blkpsm: int = 0, iteration: int = 3, useSM: bool = True,
+                  usewarmup: bool = False, warmupiteration: int = -1, isDoubleTile: bool = False,
+                  getminHeight: bool = False, *, shape: str = "3d7pt") -> int:
+    """Reference host API (j3d.cu:129): host arrays in and out, int status."""
+    if h_input.dtype not in (np.float32, np.float64) or output.dtype != h_input.dtype:
+        raise TypeError("float32 or float64 arrays of one dtype")
+    fn = N.lib().perks_j3d_iterative_f64 if h_input.dtype == np.float64 else N.lib().perks_j3d_iterative_f32
+    return fn(N.SHAPES[shape], h_input.ctypes.data, height, width_y, width_x, output.ctypes.data, bdimx,
+              blkpsm, iteration, int(useSM), int(usewarmup), warmupiteration, int(isDoubleTile),
+              int(getminHeight))
+
+
+def last_error() -> str:
+    return N.lib().perks_last_error().decode(errors="replace")
