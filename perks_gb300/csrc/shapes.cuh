@@ -3,7 +3,8 @@
 // Two evaluation orders are provided for every shape:
 //  * Ref  — the reference CPU gold order, operation by operation, with
 //           rounding intrinsics so that nvcc cannot contract a multiply and an
-//           add into an FMA. Results are bit-identical to the reference's CPU
+//           add into an FMA, and the final division by 118 / 159 done by the
+//           exact constant-division helper (divconst.cuh). Results are bit-identical to the reference's CPU
 //           code (stencil/2dstencil/<shape>/jacobi_gold_gen.cpp,
 //           stencil/3dstencil/<shape>/<shape>_gold_gen.cpp), including the
 //           mid-expression promotion to double that the reference's double
@@ -16,6 +17,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "../../include/perks.h"
+#include "divconst.cuh"
 
 namespace perks {
 
@@ -106,7 +108,7 @@ __device__ __forceinline__ T point_ref(const U& u) {
     for (int h = 0; h < H; h++) acc = O::add(acc, O::mul(T(star_e(h)), u(0, 0, 1 + h)));
 #pragma unroll
     for (int h = 0; h < H; h++) acc = O::add(acc, O::mul(T(star_n(h)), u(0, 1 + h, 0)));
-    return O::div(acc, T(118));
+    return div_const<118>(acc);
   } else if constexpr (SHAPE == PERKS_2D9PT || SHAPE == PERKS_2D25PT) {
     // Terms before the centre sum in T; the centre's double literal promotes
     // the rest of the sum to double; later products are still T products.
@@ -129,7 +131,7 @@ __device__ __forceinline__ T point_ref(const U& u) {
         }
       }
     }
-    return T(D::div(accd, 118.0));
+    return T(div_const<118>(accd));
   } else if constexpr (SHAPE == PERKS_3D7PT) {
     // e, w, n, s, t, b then minus the centre; float-literal coefficients.
     T acc = O::mul(T(0.161f), u(0, 0, 1));
@@ -173,7 +175,7 @@ __device__ __forceinline__ T point_ref(const U& u) {
     ct = O::add(ct, u(1, 1, -1));
     ct = O::add(ct, u(1, 1, 1));
     acc = D::add(acc, D::mul(0.52, double(ct)));
-    return T(D::div(acc, 159.0));
+    return T(div_const<159>(acc));
   } else if constexpr (SHAPE == PERKS_3D27PT) {
     using D = RN<double>;
     double acc = 0.0;
@@ -186,7 +188,7 @@ __device__ __forceinline__ T point_ref(const U& u) {
           const double t = D::mul(c27(z, y, x), double(u(z - 1, y - 1, x - 1)));
           acc = (z == 0 && y == 0 && x == 0) ? t : D::add(acc, t);
         }
-    return T(D::div(acc, 159.0));
+    return T(div_const<159>(acc));
   } else {  // PERKS_POISSON
     T f = O::add(u(-1, 0, 0), u(1, 0, 0));
     f = O::add(f, u(0, -1, 0));

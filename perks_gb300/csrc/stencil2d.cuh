@@ -1,372 +1,323 @@
-// 2D Jacobi time loop for sm_103a: persistent cooperative kernel with
-// shared-memory-resident rows and a bulk-copy (TMA) row pipeline.
+// 2D Jacobi time loop for sm_103a: persistent cooperative kernel in which
+// every warp streams its own column strip.
 //
-// Work decomposition (one CTA per SM):
-//   The internal field is row-major with a padded pitch (gx * TX columns).
-//   CTA (ti, tj) owns the tile of columns [tj*TX, tj*TX+TX) and rows
-//   [r0, r1) (balanced split of width_y over gy tile rows).
-//   Each step the CTA sweeps its rows in groups of R output rows. Input rows
-//   arrive in a ring of NR shared-memory slots, one cp.async.bulk per row
-//   covering the tile plus HP pad columns on each side, completing on a
-//   per-slot mbarrier. The first and last H rows of every tile always live
-//   in global memory, so neighbouring tiles read their halos straight from
-//   the field.
-//   PERKS caching: tile rows [r0+H, r0+H+C) stay in shared memory for the
-//   whole launch ("resident rows"). They are updated in place with a skew:
-//   the output of a row goes into the slot of the row R+H positions behind it
-//   in the sweep (dead by then), so no extra buffer or barrier is needed. The
-//   resident rows' first and last HP columns are also stored to the field so
-//   that the left/right neighbour tiles can load them as pads.
-//   Steps are separated by a bounded grid barrier.
+// Work decomposition:
+//   The internal field is row-major with pitch = ns * SW columns, SW = 32*V
+//   (V elements = 16 bytes per lane). Warp w of the grid owns strip s and row
+//   band b: columns [s*SW, s*SW+SW), rows [r0, r1). Adjacent strips of one
+//   band sit in the same CTA.
+//   Each step the warp sweeps its band row by row. Rows are fetched with
+//   cp.async.cg (16 bytes per lane, plus one 16-byte chunk per edge lane for
+//   the H columns left and right of the strip) into a private ring of DR
+//   shared-memory slots, D rows ahead of use; the vertical window of 2H+1 rows
+//   lives in registers and horizontal neighbours move between lanes by warp
+//   shuffles. Nothing synchronises the block inside a step: warps exchange
+//   halos only through the field in global memory, and steps are separated by
+//   one bounded grid barrier.
+//   PERKS caching: rows [r0+H, r0+H+C) of every band stay in shared memory for
+//   the whole launch. Each lane owns its V columns of those rows, reads them
+//   into its register window before overwriting them, and so updates them in
+//   place; the strip's first and last H columns of those rows are also stored
+//   to the field, where the neighbouring strips read them as halo.
 //   With `alternate`, odd steps sweep bottom-up so that the rows written last
-//   are read first (still in L2), and input lines that are dead after their
-//   last read are dropped from L2 without write-back.
+//   are read first (from L2); interior lines of interior rows are loaded with
+//   an evict-first policy and dropped from L2 without write-back once read
+//   (they are dead until the next step overwrites them).
 //
-// Boundary: clamp-to-edge as the reference. Rows outside the domain alias the
-// edge row's slot; columns outside the domain are filled in shared memory
-// from the edge column ("fixups") before the rows are read.
+// Boundary: clamp-to-edge as the reference (row and edge-column indices are
+// clamped; elements of the last strip beyond width_x take the value of column
+// width_x-1), or Dirichlet (outer H cells keep their input value).
 #pragma once
 #include <cstdint>
+#include <type_traits>
 #include "ptx.cuh"
 #include "shapes.cuh"
 
 namespace perks {
 
 struct Stencil2DParams {
-  void* f[2];         // internal fields, pitch elements per row
-  int wy, wx, pitch;  // domain and padded row pitch (elements)
-  int gx, gy;         // tile grid
-  int steps;          // steps run by this launch
-  int t0;             // global index of this launch's first step
-  int C;              // resident rows per tile (upper bound; tiles clamp to TY-2H)
-  int M;              // resident slots (C + R + H), 0 when C == 0
-  int dirichlet;      // hold the outer H cells fixed instead of clamping
-  int alternate;      // alternate sweep direction + L2 line dropping
-  int persistent;     // grid barrier between steps (cooperative launch)
-  unsigned* bar;      // grid barrier words [2]
-  unsigned* status;   // error word
+  void* f[2];        // internal fields, pitch elements per row
+  int wy, wx, pitch; // domain and padded row pitch (elements)
+  int ns, nb;        // strips and bands
+  int steps, t0;     // steps in this launch, global index of its first step
+  int C;             // resident rows per warp (0 = none)
+  int dirichlet, alternate, persistent;
+  unsigned* bar;     // grid barrier words [2]
+  unsigned* status;  // error word
 };
 
-template <class T, int SHAPE, int NT_>
+template <class T, int SHAPE>
 struct Cfg2D {
   static constexpr int H = ShapeInfo<SHAPE>::H;
   static constexpr bool BOX = ShapeInfo<SHAPE>::box;
-  static constexpr int NT = NT_;
-  static constexpr int V = 16 / sizeof(T);            // elements per 16-byte vector
-  static constexpr int TX = NT * V;                    // tile width
-  static constexpr int HP = ((H + V - 1) / V) * V;     // pad columns (16-byte multiple)
-  static constexpr int RW = TX + 2 * HP;               // shared-memory row width
-  static constexpr int R = BOX ? 4 : 8;                // output rows per group
-  static constexpr int NR = 2 * R + 2 * H + (BOX ? 8 : 4);  // ring slots (>= 2R + 2H)
-  static constexpr int NVW = (V + 2 * HP) / V;         // vectors per full window row
-  static_assert(NR <= 64, "phase mask holds 64 slots");
-  static constexpr size_t ring_bytes = size_t(NR) * RW * sizeof(T);
-  static constexpr size_t row_bytes = size_t(RW) * sizeof(T);
-  static constexpr size_t bar_bytes = (NR + 2) * sizeof(uint64_t);
+  static constexpr int V = 16 / sizeof(T);               // elements per lane
+  static constexpr int SW = 32 * V;                      // strip width
+  static constexpr int WN = 2 * H + 1;                   // window rows
+  // registers the window needs (32-bit words), to pick 1024 or 512 threads
+  static constexpr int REG_EST =
+      int(sizeof(T) / 4) * (BOX ? WN * (V + 2 * H) + V : WN * (V + 1) + (V + 2 * H) + V) + 40;
+  // warps per CTA: as many as the register file allows (1024/768/512/256 threads)
+  static constexpr int NW = (REG_EST <= 64 && !BOX) ? 32 : REG_EST <= 80 ? 24 : REG_EST <= 110 ? 16 : 8;
+  static constexpr int NT = NW * 32;
+  static constexpr int D = 96 / NW;                      // rows in flight per warp (~48 KB per SM)
+  static constexpr int DR = D + 1;                       // ring slots per warp
+  static constexpr int EL = (2 * H + 0);                 // edge lanes
+  static constexpr int SLOT = SW + EL * V;               // ring slot: strip row + edge chunks
+  static constexpr size_t ring_bytes = size_t(NW) * DR * SLOT * sizeof(T);
+  static constexpr size_t res_row_bytes = size_t(NW) * SW * sizeof(T);  // one resident row for every warp
+  static_assert(2 * H <= 32, "edge lanes");
 };
 
-template <class T>
-struct Vec;
-template <>
-struct Vec<float> {
-  using type = float4;
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, uint64_t pol) {
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(smem_u32(smem)), "l"(gmem),
+               "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ void unpack(const float4& v, float (&o)[4]) {
+  o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+__device__ __forceinline__ void unpack(const double2& v, double (&o)[2]) {
+  o[0] = v.x; o[1] = v.y;
+}
+template <class VT, class T, int N>
+__device__ __forceinline__ VT pack(const T (&o)[N]) {
+  if constexpr (N == 4) return make_float4(o[0], o[1], o[2], o[3]);
+  else return make_double2(o[0], o[1]);
+}
+
+// A window row in registers: V values of this lane and one edge value.
+template <class T, int V>
+struct Row2D {
+  T v[V];
+  T e;
 };
-template <>
-struct Vec<double> {
-  using type = double2;
+template <class T, int N>
+struct Win2D {
+  T h[N];
 };
 
-template <class T, int SHAPE, bool FAST, int NT>
-__global__ void __launch_bounds__(NT, 1) stencil2d_kernel(const __grid_constant__ Stencil2DParams p) {
-  using Cf = Cfg2D<T, SHAPE, NT>;
-  using VT = typename Vec<T>::type;
-  constexpr int H = Cf::H, V = Cf::V, TX = Cf::TX, HP = Cf::HP, RW = Cf::RW, R = Cf::R, NR = Cf::NR;
-  constexpr int WROWS = R + 2 * H;     // window rows per group
-  constexpr int NVW = Cf::NVW;
-  constexpr int WW = V + 2 * HP;       // window width (elements)
+// Compile-time loop: f(std::integral_constant<int, i>) for i = 0..N-1, so that
+// register-array indices derived from i are constants.
+template <int N, class F>
+__device__ __forceinline__ void static_for(F&& f) {
+  if constexpr (N > 0) {
+    static_for<N - 1>(f);
+    f(std::integral_constant<int, N - 1>{});
+  }
+}
+
+template <class T, int SHAPE, bool FAST>
+__global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const __grid_constant__ Stencil2DParams p) {
+  using Cf = Cfg2D<T, SHAPE>;
+  using VT = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  constexpr int H = Cf::H, V = Cf::V, SW = Cf::SW, NW = Cf::NW, D = Cf::D, DR = Cf::DR, SLOT = Cf::SLOT;
+  constexpr int WN = Cf::WN;
+  constexpr bool BOX = Cf::BOX;
+  constexpr int WW = V + 2 * H;  // horizontal window of one row
+  using RowT = Row2D<T, V>;
+  using WinT = Win2D<T, WW>;
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  T* ring = reinterpret_cast<T*>(smem_raw);
-  T* res = ring + NR * RW;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(res + size_t(p.M) * RW);
-  uint64_t* bar_res = bars + NR;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  T* ring = reinterpret_cast<T*>(smem_raw) + size_t(wid) * DR * SLOT;
+  T* res = reinterpret_cast<T*>(smem_raw + Cf::ring_bytes);  // [C][NW][SW]
 
-  const int tid = threadIdx.x;
-  const int ti = blockIdx.x / p.gx, tj = blockIdx.x % p.gx;
-  const int r0 = int((long long)ti * p.wy / p.gy);
-  const int r1 = int((long long)(ti + 1) * p.wy / p.gy);
-  const int TY = r1 - r0;
-  const int x0 = tj * TX;
-  const int C = (p.M > 0) ? max(0, min(p.C, TY - 2 * H)) : 0;
-  const int rres0 = r0 + H;
-  const int M = p.M;
   const int wy = p.wy, wx = p.wx, pitch = p.pitch;
-  const bool left_edge = (tj == 0) && !p.dirichlet;
-  const bool right_edge = (tj == p.gx - 1) && !p.dirichlet;
-  const int lw = wx - 1 - x0;  // tile-local index of the last domain column (right edge tile)
-  // Source window of one row copy: [x0-HP, x0+TX+HP) clipped to the pitch.
-  const int src_lo = max(x0 - HP, 0);
-  const int src_hi = min(x0 + TX + HP, pitch);
-  const int dst_off = src_lo - (x0 - HP);
-  const unsigned copy_bytes = unsigned(src_hi - src_lo) * sizeof(T);
-  const bool has_w = x0 - HP >= 0, has_e = x0 + TX + HP <= pitch;
+  const int item = blockIdx.x * NW + wid;
+  const bool active = item < p.ns * p.nb;
+  const int strip = active ? item % p.ns : 0;
+  const int band = active ? item / p.ns : 0;
+  const int x0 = strip * SW;
+  const int r0 = int((long long)band * wy / p.nb), r1 = int((long long)(band + 1) * wy / p.nb);
+  const int TY = r1 - r0;
+  const int C = active ? max(0, min(p.C, TY - 2 * H)) : 0;
+  const int rres0 = r0 + H;
+  const int xl = x0 + lane * V;            // this lane's first column
+  const bool dir = p.dirichlet != 0;
+  const bool ghost_strip = (x0 + SW > wx) && !dir;  // strip reaches past the last column
+  const int lw = wx - 1 - x0;              // strip-local last column
+  // Edge lanes: lane k < H needs column x0-1-k, lane H+k needs x0+SW+k, both
+  // clamped to the domain (this is the reference's clamp boundary). Each edge
+  // lane fetches the aligned 16-byte chunk holding its column.
+  const bool edge_lane = lane < 2 * H;
+  const int edge_col = lane < H ? max(x0 - 1 - lane, 0) : min(x0 + SW + (lane - H), wx - 1);
+  const int edge_chunk = (edge_col / V) * V;
+  const int edge_sub = edge_col - edge_chunk;
 
-  GridBarrier gbar{p.bar, p.status, gridDim.x * gridDim.y * gridDim.z};
+  GridBarrier gbar{p.bar, p.status, gridDim.x};
   const uint64_t pol = policy_evict_normal();
   const uint64_t pol_first = policy_evict_first();
-
-  if (tid == 0) {
-    for (int i = 0; i < NR + 1; i++) mbar_init(&bars[i], 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-
-  uint64_t phase = 0ull;    // per ring slot parity (identical in every thread)
-  uint32_t res_phase = 0u;
-  int off = 0;             // resident skew (mod M)
   bool ok = true;
-  int issued = 0, waited = 0;  // sweep positions issued / waited this step (drain on error)
-  bool fwd = true;
 
-  auto slot_of_res = [&](int r) -> T* {
-    int s = (r - rres0 + off) % M;
-    if (s < 0) s += M;
-    return res + size_t(s) * RW;
-  };
-  auto fixup_row = [&](T* slot, int which) {
-    // which 0: left edge, 1: right edge. Columns outside the domain take the
-    // value of the edge column.
-    if (which == 0) {
-      const T v = slot[HP];
-#pragma unroll
-      for (int k = 1; k <= H; k++) slot[HP - k] = v;
-    } else {
-      const T v = slot[HP + lw];
-#pragma unroll
-      for (int k = 1; k <= H; k++) slot[HP + lw + k] = v;
-    }
-  };
+  auto res_ptr = [&](int r) -> T* { return res + (size_t(r - rres0) * NW + wid) * SW + lane * V; };
+  auto is_res = [&](int r) { return r >= rres0 && r < rres0 + C; };
 
-  // ---------------------------------------------------------------- prologue
-  // Bring the resident rows in from the field once per launch.
   if (C > 0) {
     const T* fin = static_cast<const T*>(p.f[p.t0 & 1]);
-    if (tid == 0) {
-      mbar_arrive_expect_tx(bar_res, copy_bytes * unsigned(C));
-      for (int r = rres0; r < rres0 + C; r++)
-        bulk_g2s(slot_of_res(r) + dst_off, fin + size_t(r) * pitch + src_lo, copy_bytes, bar_res, pol);
-    }
-    if (!mbar_wait(bar_res, res_phase & 1u)) {
-      atomicOr(p.status, kErrCopyTimeout);
-      ok = false;
-    }
-    res_phase ^= 1u;
-    ok = __syncthreads_and(ok);
+    for (int k = 0; k < C; k++)
+      *reinterpret_cast<VT*>(res_ptr(rres0 + k)) = *reinterpret_cast<const VT*>(fin + size_t(rres0 + k) * pitch + xl);
   }
 
   for (int it = 0; it < p.steps && ok; it++) {
     const int t = p.t0 + it;
     const T* fin = static_cast<const T*>(p.f[t & 1]);
     T* fout = static_cast<T*>(p.f[(t + 1) & 1]);
-    fwd = !p.alternate || ((t & 1) == 0);
-    // Row of sweep position s (positions -H..TY+H-1 include the halo rows).
-    auto row_of = [&](int s) { return fwd ? r0 + s : r1 - 1 - s; };
-    auto is_res = [&](int r) { return C > 0 && r >= rres0 && r < rres0 + C; };
-    auto loaded = [&](int s) {
-      const int r = row_of(s);
-      return r >= 0 && r < wy && !is_res(r);
-    };
-    auto pos_of = [&](int r) { return fwd ? r - r0 : r1 - 1 - r; };
-    auto slot_of = [&](int r) -> T* {
-      // shared-memory slot holding input row r (clamped to the domain)
-      r = min(max(r, 0), wy - 1);
-      if (is_res(r)) return slot_of_res(r);
-      const int s = pos_of(r);
-      return ring + size_t((s + H) % NR) * RW;
-    };
+    const bool fwd = !p.alternate || ((t & 1) == 0);
 
-    issued = -H;  // next sweep position the producer will issue
-    auto produce = [&](int upto) {
-      // thread 0 only: issue row copies for positions < upto
-      const int lim = min(upto, TY + H);
-      for (; issued < lim; issued++) {
-        if (!loaded(issued)) continue;
-        const int r = row_of(issued);
-        uint64_t* b = &bars[(issued + H) % NR];
-        T* dst = ring + size_t((issued + H) % NR) * RW + dst_off;
-        mbar_arrive_expect_tx(b, copy_bytes);
-        // interior rows are read only by this CTA: evict them first from L2
-        const bool interior = r >= r0 + H && r < r1 - H;
-        bulk_g2s(dst, fin + size_t(r) * pitch + src_lo, copy_bytes, b,
-                 (p.alternate && interior) ? pol_first : pol);
-      }
-    };
-
-    if (tid == 0) {
-      fence_proxy_async_global();
-      produce(NR - H);
-      if (C > 0 && it > 0 && (has_w || has_e)) {
-        // refresh the resident rows' pad columns from the neighbours' stores
-        const unsigned pb = HP * sizeof(T);
-        mbar_arrive_expect_tx(bar_res, pb * unsigned(C) * unsigned(has_w + has_e));
-        for (int r = rres0; r < rres0 + C; r++) {
-          T* s = slot_of_res(r);
-          if (has_w) bulk_g2s(s, fin + size_t(r) * pitch + x0 - HP, pb, bar_res, pol);
-          if (has_e) bulk_g2s(s + HP + TX, fin + size_t(r) * pitch + x0 + TX, pb, bar_res, pol);
+    if (active) {
+      auto row_of = [&](int q) { return min(max(fwd ? r0 + q : r1 - 1 - q, 0), wy - 1); };
+      auto slot_of = [&](int q) -> T* { return ring + size_t((q + 2 * DR) % DR) * SLOT; };
+      auto interior = [&](int r) { return p.alternate && r >= r0 + H && r < r1 - H; };
+      // Issue the copies for sweep position q (one commit group per position).
+      auto fetch = [&](int q) {
+        if (q < TY + H) {
+          T* slot = slot_of(q);
+          const int r = row_of(q);
+          const T* src = fin + size_t(r) * pitch;
+          if (!is_res(r)) cp_async16(slot + lane * V, src + xl, interior(r) ? pol_first : pol);
+          if (edge_lane) cp_async16(slot + SW + lane * V, src + edge_chunk, pol);
         }
-      }
-    }
-    if (C > 0 && it > 0 && (has_w || has_e)) {
-      if (!mbar_wait(bar_res, res_phase & 1u)) {
-        atomicOr(p.status, kErrCopyTimeout);
-        ok = false;
-      }
-      res_phase ^= 1u;
-      ok = __syncthreads_and(ok);
-      if (!ok) break;
-    }
-    if (C > 0 && (left_edge || right_edge)) {
-      for (int k = tid; k < C; k += NT) {
-        T* s = slot_of_res(rres0 + k);
-        if (left_edge) fixup_row(s, 0);
-        if (right_edge) fixup_row(s, 1);
-      }
-    }
-
-    waited = -H;
-    for (int lo = 0; lo < TY && ok; lo += R) {
-      const int hi = min(lo + R, TY);
-      const int need_hi = hi + H;
-      for (; waited < need_hi; waited++) {
-        if (!loaded(waited)) continue;
-        const int q = (waited + H) % NR;
-        if (!mbar_wait(&bars[q], unsigned(phase >> q) & 1u)) {
-          atomicOr(p.status, kErrCopyTimeout);
-          ok = false;
-          break;
+        cp_async_commit();
+      };
+      // Move position q from the ring (or resident storage) into registers.
+      auto load_row = [&](int q) -> RowT {
+        RowT out;
+        const T* slot = slot_of(q);
+        const int r = row_of(q);
+        const bool rr = is_res(r);
+        const T* vsrc = rr ? res_ptr(r) : slot + lane * V;  // one load from whichever holds the row
+        const VT v = *reinterpret_cast<const VT*>(vsrc);
+        unpack(v, out.v);
+        out.e = edge_lane ? slot[SW + lane * V + edge_sub] : T(0);  // only edge lanes own an edge chunk
+        if (ghost_strip) {
+          // elements beyond the last column take that column's value
+          const int le = lw % V;
+          T edge = out.v[0];
+#pragma unroll
+          for (int i = 1; i < V; i++) edge = (le == i) ? out.v[i] : edge;
+          edge = __shfl_sync(0xffffffffu, edge, min(lw / V, 31));
+          const int lim = lw - lane * V;  // elements i > lim are beyond the domain
+#pragma unroll
+          for (int i = 0; i < V; i++) out.v[i] = (i > lim) ? edge : out.v[i];
         }
-        phase ^= (1ull << q);
-        T* slot = ring + size_t(q) * RW;
-        if (left_edge && tid == (waited & 31)) fixup_row(slot, 0);
-        if (right_edge && tid == 32 + (waited & 31)) fixup_row(slot, 1);
-      }
-      ok = __syncthreads_and(ok);
-      if (!ok) break;
-      if (tid == 0) produce(lo - H + NR);
-
-      // rows of this group in increasing row order
-      const int ra = fwd ? r0 + lo : r1 - hi;   // first output row
-      const int nrows = hi - lo;
-      const int c0 = tid * V;  // window start in slot coordinates (= column x0 + c0 - HP)
-      // Star shapes: the middle V columns of every window row stay in
-      // registers; the full-width window of each centre row is loaded just
-      // before its outputs are computed. Box shapes keep full windows.
-      constexpr int WCOL = Cf::BOX ? WW : V;
-      constexpr int WOFF = Cf::BOX ? 0 : HP;   // slot column of w[.][0] relative to c0
-      T w[WROWS][WCOL];
-#pragma unroll
-      for (int i = 0; i < WROWS; i++) {
-        if (i < nrows + 2 * H) {
-          const T* s = slot_of(ra - H + i) + c0 + WOFF;
-#pragma unroll
-          for (int v = 0; v < WCOL / V; v++) {
-            VT x = reinterpret_cast<const VT*>(s)[v];
-            const T* xe = reinterpret_cast<const T*>(&x);
-#pragma unroll
-            for (int e = 0; e < V; e++) w[i][v * V + e] = xe[e];
-          }
+        if (!rr && interior(r)) {
+          // the middle lines of this strip row are dead once read: drop them
+          // from L2 without write-back (edge lines stay: neighbours read them)
+          __syncwarp();
+          constexpr int LE = 128 / int(sizeof(T));  // elements per 128-byte line
+          constexpr int LPL = LE / V;               // lanes per line
+          const int c = lane * V;
+          if ((lane % LPL) == 0 && c >= LE && c + LE <= SW - LE) l2_discard_line(fin + size_t(r) * pitch + x0 + c);
         }
-      }
+        return out;
+      };
+
+      // Star shapes keep V values (+ one edge value) per window row and build
+      // the horizontal window of the centre row when it is needed; box shapes
+      // build each row's horizontal window once, when the row arrives.
+      RowT w[BOX ? 1 : WN];       // star: window rows, slot (position + H) mod WN
+      WinT wf[BOX ? WN : 1];      // box: full horizontal window of each row
+      // Horizontal window of one row: own V values and H neighbours on each
+      // side, from the neighbouring lanes or, at the strip edge, the edge lanes.
+      auto hwin = [&](const RowT r) -> WinT {
+        WinT out;
 #pragma unroll
-      for (int k = 0; k < R; k++) {
-        if (k < nrows) {
-          const int y = ra + k;
-          T cw[Cf::BOX ? 1 : WW];
-          if constexpr (!Cf::BOX) {
-            const T* s = slot_of(y) + c0;
+        for (int i = 0; i < V; i++) out.h[H + i] = r.v[i];
 #pragma unroll
-            for (int v = 0; v < NVW; v++) {
-              VT x = reinterpret_cast<const VT*>(s)[v];
-              const T* xe = reinterpret_cast<const T*>(&x);
+        for (int d = 1; d <= H; d++) {
+          const int dl = (d + V - 1) / V;  // lanes away
+          const T vin = __shfl_up_sync(0xffffffffu, r.v[dl * V - d], dl);
+          const T ved = __shfl_sync(0xffffffffu, r.e, max(d - 1 - lane * V, 0));
+          out.h[H - d] = (lane * V >= d) ? vin : ved;
+          const T vin2 = __shfl_down_sync(0xffffffffu, r.v[(d - 1) % V], dl);
+          const T ved2 = __shfl_sync(0xffffffffu, r.e, H + max(d - 1 - (31 - lane) * V, 0));
+          out.h[H + V - 1 + d] = ((31 - lane) * V >= d) ? vin2 : ved2;
+        }
+        return out;
+      };
+      auto bring = [&](int q, auto kc) {
+        constexpr int k = decltype(kc)::value;  // window slot
+        if constexpr (BOX) wf[k] = hwin(load_row(q));
+        else w[k] = load_row(q);
+      };
+      for (int q = -H; q < -H + D; q++) fetch(q);
+      int qn = -H;  // next position to bring into the window
+      static_for<2 * H>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        cp_async_wait<D - 1>();
+        __syncwarp();
+        bring(qn, kc);
+        fetch(qn + D);
+        qn++;
+      });
+
+      auto step_rows = [&](auto fwd_c) {
+        constexpr bool F = decltype(fwd_c)::value;
+        for (int q0 = 0; q0 < TY; q0 += WN) {
+          static_for<WN>([&](auto jc) {
+            constexpr int j = decltype(jc)::value;
+            const int q = q0 + j;
+            if (q < TY) {
+              cp_async_wait<D - 1>();
+              __syncwarp();
+              bring(qn, std::integral_constant<int, (j + 2 * H) % WN>{});
+              fetch(qn + D);
+              qn++;
+              const int y = F ? r0 + q : r1 - 1 - q;
+              // window slot of row y+dy
+              auto ws = [](int dy) constexpr { return (j + H + (F ? dy : -dy) + 2 * WN) % WN; };
+              WinT hc;  // star: horizontal window of the centre row
+              if constexpr (!BOX) hc = hwin(w[ws(0)]);
+              T o[V];
 #pragma unroll
-              for (int e = 0; e < V; e++) cw[v * V + e] = xe[e];
+              for (int i = 0; i < V; i++) {
+                auto u = [&](int, int dy, int dx) -> T {
+                  if constexpr (BOX) return wf[ws(dy)].h[H + i + dx];
+                  else return dy == 0 ? hc.h[H + i + dx] : w[ws(dy)].v[i];
+                };
+                o[i] = stencil_point<T, SHAPE, FAST>(u);
+              }
+              if (dir) {
+                const bool row_fixed = y < H || y >= wy - H;
+#pragma unroll
+                for (int i = 0; i < V; i++) {
+                  const int x = xl + i;
+                  T old;
+                  if constexpr (BOX) old = wf[ws(0)].h[H + i];
+                  else old = w[ws(0)].v[i];
+                  if (row_fixed || x < H || x >= wx - H) o[i] = old;
+                }
+              }
+              const VT ov = pack<VT>(o);
+              if (is_res(y)) {
+                *reinterpret_cast<VT*>(res_ptr(y)) = ov;
+                if (lane * V < H || (lane + 1) * V > SW - H) *reinterpret_cast<VT*>(fout + size_t(y) * pitch + xl) = ov;
+              } else {
+                *reinterpret_cast<VT*>(fout + size_t(y) * pitch + xl) = ov;
+              }
             }
-          }
-          T o[V];
-#pragma unroll
-          for (int e = 0; e < V; e++) {
-            auto u = [&](int, int dy, int dx) -> T {
-              if constexpr (Cf::BOX) return w[k + H + dy][HP + e + dx];
-              else return dy == 0 ? cw[HP + e + dx] : w[k + H + dy][e];
-            };
-            o[e] = stencil_point<T, SHAPE, FAST>(u);
-          }
-          if (p.dirichlet) {
-            const bool row_fixed = (y < H) || (y >= wy - H);
-#pragma unroll
-            for (int e = 0; e < V; e++) {
-              const int x = x0 + c0 + e;
-              const T old = Cf::BOX ? w[k + H][HP + e] : w[k + H][e];
-              if (row_fixed || x < H || x >= wx - H) o[e] = old;
-            }
-          }
-          VT ov;
-          T* oe = reinterpret_cast<T*>(&ov);
-#pragma unroll
-          for (int e = 0; e < V; e++) oe[e] = o[e];
-          if (is_res(y)) {
-            // in-place update with skew: the slot of the row R+H positions behind
-            const int tr = fwd ? y - (R + H) : y + (R + H);
-            int s = (tr - rres0 + off) % M;
-            if (s < 0) s += M;
-            *reinterpret_cast<VT*>(res + size_t(s) * RW + HP + c0) = ov;
-            if (c0 < HP || c0 >= TX - HP)
-              *reinterpret_cast<VT*>(fout + size_t(y) * pitch + x0 + c0) = ov;
-          } else {
-            *reinterpret_cast<VT*>(fout + size_t(y) * pitch + x0 + c0) = ov;
-          }
+          });
         }
-      }
+      };
+      if (fwd) step_rows(std::true_type{});
+      else step_rows(std::false_type{});
+      cp_async_wait<0>();
+      __syncwarp();
     }
-    if (!ok) break;
-    // Every issued copy has been waited for (positions up to TY+H-1).
-    off = fwd ? off - (R + H) : off + (R + H);
-    off %= (M > 0 ? M : 1);
-    if (off < 0) off += M;
-    if (it + 1 < p.steps) {
-      fence_proxy_async_global();
-      if (p.persistent) {
-        if (!gbar.sync()) { ok = false; break; }
-      }
+    if (it + 1 < p.steps && p.persistent) {
+      if (!gbar.sync()) ok = false;
     }
   }
-  // ---------------------------------------------------------------- epilogue
   if (ok && C > 0) {
-    __syncthreads();
     T* fnew = static_cast<T*>(p.f[(p.t0 + p.steps) & 1]);
-    for (int k = 0; k < C; k++) {
-      const int r = rres0 + k;
-      *reinterpret_cast<VT*>(fnew + size_t(r) * pitch + x0 + tid * V) =
-          *reinterpret_cast<const VT*>(slot_of_res(r) + HP + tid * V);
-    }
-  }
-  if (!ok) {
-    // Leave no bulk copy in flight into this CTA's shared memory: thread 0
-    // waits (bounded) for every position it issued that was not yet waited.
-    __syncthreads();
-    if (tid == 0) {
-      uint64_t ph = phase;
-      for (int s = waited; s < issued; s++) {
-        const int r = fwd ? r0 + s : r1 - 1 - s;
-        if (r < 0 || r >= wy || (C > 0 && r >= rres0 && r < rres0 + C)) continue;
-        const int q = (s + H) % NR;
-        long long tw = clock64();
-        while (!mbar_try_wait(&bars[q], unsigned(ph >> q) & 1u)) {
-          if (clock64() - tw > (1ll << 28)) break;
-        }
-        ph ^= (1ull << q);
-      }
-    }
+    for (int k = 0; k < C; k++)
+      *reinterpret_cast<VT*>(fnew + size_t(rres0 + k) * pitch + xl) = *reinterpret_cast<const VT*>(res_ptr(rres0 + k));
   }
 }
 

@@ -8,47 +8,45 @@
 
 namespace perks {
 
-constexpr int kNT2D = 256;
 
 inline int ceil_div(long long a, long long b) { return int((a + b - 1) / b); }
 
 template <class T, int SHAPE, bool FAST>
 int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int wy, int wx, int steps,
                      perks_stencil_stats* st) {
-  using Cf = Cfg2D<T, SHAPE, kNT2D>;
-  constexpr int H = Cf::H, R = Cf::R;
+  using Cf = Cfg2D<T, SHAPE>;
+  constexpr int H = Cf::H;
   const DeviceInfo* dev = device_info();
   if (!dev) return PERKS_ERR_NO_DEVICE;
   cudaStream_t s = static_cast<cudaStream_t>(o.stream);
   const bool persistent = o.kernel == PERKS_KERNEL_PERSISTENT;
   const int ctas = o.ctas > 0 ? std::min(o.ctas, dev->sms) : dev->sms;
-  const int gx = ceil_div(wx, Cf::TX);
-  if (gx > ctas)
+  const long long warps = (long long)ctas * Cf::NW;
+  const int ns = ceil_div(wx, Cf::SW);
+  if (ns > warps)
     return fail(PERKS_ERR_UNSUPPORTED, "width_x " + std::to_string(wx) + " needs more than " +
-                                           std::to_string(ctas) + " column tiles");
-  const int gy = std::max(1, std::min(ctas / gx, wy));
-  const int pitch = gx * Cf::TX;
-  const int tymax = ceil_div(wy, gy);
+                                           std::to_string(warps) + " column strips");
+  const int nb = int(std::max<long long>(1, std::min<long long>(warps / ns, wy)));
+  const int pitch = ns * Cf::SW;
+  const int tymax = ceil_div(wy, nb);
+  const int grid = ceil_div((long long)ns * nb, Cf::NW);
 
-  size_t fixed = Cf::ring_bytes + Cf::bar_bytes;
-  int C = 0, M = 0;
+  int C = 0;
   if (persistent && o.cache_rows != 0 && steps > 1) {
-    long long avail = (long long)dev->smem_optin - (long long)fixed - 256;
-    int cmax = int(avail / (long long)Cf::row_bytes) - (R + H);
+    long long avail = (long long)dev->smem_optin - (long long)Cf::ring_bytes - 256;
+    int cmax = int(std::max<long long>(0, avail / (long long)Cf::res_row_bytes));
     if (o.cache_rows > 0) cmax = std::min(cmax, o.cache_rows);
-    C = std::min(cmax, tymax - 2 * H);
-    if (C <= 0) C = 0;
-    M = C > 0 ? C + R + H : 0;
+    C = std::max(0, std::min(cmax, tymax - 2 * H));
   }
-  const size_t smem = fixed + size_t(M) * Cf::row_bytes;
+  const size_t smem = Cf::ring_bytes + size_t(C) * Cf::res_row_bytes;
   if (smem > dev->smem_optin) return fail(PERKS_ERR_UNSUPPORTED, "shared memory budget exceeded");
 
   if (st) {
     *st = perks_stencil_stats{};
-    st->grid_x = gx;
-    st->grid_y = gy;
+    st->grid_x = ns;
+    st->grid_y = nb;
     st->grid_z = 1;
-    st->tile_x = Cf::TX;
+    st->tile_x = Cf::SW;
     st->tile_y = tymax;
     st->cached_rows = C;
   }
@@ -77,19 +75,17 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   p.wy = wy;
   p.wx = wx;
   p.pitch = pitch;
-  p.gx = gx;
-  p.gy = gy;
+  p.ns = ns;
+  p.nb = nb;
   p.C = C;
-  p.M = M;
   p.dirichlet = o.boundary == PERKS_BOUNDARY_DIRICHLET;
   p.alternate = persistent && o.l2_sweep;
   p.persistent = persistent;
   p.bar = sw.bar;
   p.status = sw.status;
 
-  auto kern = stencil2d_kernel<T, SHAPE, FAST, kNT2D>;
+  auto kern = stencil2d_kernel<T, SHAPE, FAST>;
   PERKS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  const int grid = gx * gy;
   cudaEvent_t e0, e1;
   PERKS_CUDA(cudaEventCreate(&e0));
   PERKS_CUDA(cudaEventCreate(&e1));
@@ -97,7 +93,7 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   int launches = 0;
   if (persistent) {
     int nb = 0;
-    PERKS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kNT2D, smem));
+    PERKS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, Cf::NT, smem));
     if (nb * dev->sms < grid) {
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
@@ -107,7 +103,7 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
     p.steps = steps;
     p.t0 = 0;
     void* args[] = {&p};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kNT2D), args, smem, s);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(Cf::NT), args, smem, s);
     if (e != cudaSuccess) {
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
@@ -118,7 +114,7 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
     p.steps = 1;
     for (int t = 0; t < steps; t++) {
       p.t0 = t;
-      kern<<<grid, kNT2D, smem, s>>>(p);
+      kern<<<grid, Cf::NT, smem, s>>>(p);
     }
     launches = steps;
     cudaError_t e = cudaGetLastError();
@@ -142,8 +138,8 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
     st->ms = ms;
     st->gcells_per_s = double(elems) * steps / (double(ms) * 1e6);
     long long cached = 0;
-    for (int ti = 0; ti < gy; ti++) {
-      int r0 = int((long long)ti * wy / gy), r1 = int((long long)(ti + 1) * wy / gy);
+    for (int b = 0; b < nb; b++) {
+      int r0 = int((long long)b * wy / nb), r1 = int((long long)(b + 1) * wy / nb);
       cached += std::max(0, std::min(C, r1 - r0 - 2 * H));
     }
     st->cached_fraction = double(cached) / double(wy);
