@@ -120,6 +120,19 @@ PERKS_API int perks_stencil2d(const perks_stencil_opts* opts, const void* d_in, 
 PERKS_API int perks_stencil3d(const perks_stencil_opts* opts, const void* d_in, void* d_out, int height,
                     int width_y, int width_x, int steps, perks_stencil_stats* stats);
 
+/* perks_stencil2d for callers that cannot allocate device memory (programs
+ * that fix their device-memory footprint at start-up, or run under another
+ * framework's memory manager, and may not call cudaMalloc mid-run). No
+ * counterpart in the reference. Same arguments and results as
+ * perks_stencil2d (reference evaluation order only), but all scratch comes
+ * from one 32 MiB static device array inside the library: fields needing more
+ * (2 * width_y * padded width * sizeof(REAL) + 256 bytes) are rejected with
+ * PERKS_ERR_INVALID_ARG. The first call on a device resolves the array's
+ * address and should come before any stream capture. Calls share the array:
+ * calls whose GPU work overlaps race and must not be issued. */
+PERKS_API int perks_stencil2d_noalloc(const perks_stencil_opts* opts, const void* d_in, void* d_out,
+                                      int width_y, int width_x, int steps, perks_stencil_stats* stats);
+
 /* Host-buffer drop-ins with the reference's argument list. The stencil shape
  * is the first argument (the reference fixes it per executable with -D
  * macros). bdimx/blkpsm/async/useSM/isDoubleTile keep their meaning where

@@ -63,6 +63,8 @@ SIGNATURES = {
                                 ctypes.POINTER(StencilStats)]),
     "perks_stencil3d": (c_int, [ctypes.POINTER(StencilOpts), c_void_p, c_void_p, c_int, c_int, c_int, c_int,
                                 ctypes.POINTER(StencilStats)]),
+    "perks_stencil2d_noalloc": (c_int, [ctypes.POINTER(StencilOpts), c_void_p, c_void_p, c_int, c_int, c_int,
+                                        ctypes.POINTER(StencilStats)]),
     "perks_jacobi_iterative_f32": (c_int, [c_int, c_void_p, c_int, c_int, c_void_p] + [c_int] * 8),
     "perks_jacobi_iterative_f64": (c_int, [c_int, c_void_p, c_int, c_int, c_void_p] + [c_int] * 8),
     "perks_j3d_iterative_f32": (c_int, [c_int, c_void_p, c_int, c_int, c_int, c_void_p] + [c_int] * 8),
