@@ -7,9 +7,10 @@ this package is its ctypes host mirror.
 from . import _native
 from ._native import PerksError, SHAPES, HALO, lib
 from .stencil import j3d_iterative, jacobi_iterative, last_error, stencil2d, stencil3d
+from .cg import cg_csr, cg_dia, spmv_csr, spmv_dia
 
 __all__ = ["PerksError", "SHAPES", "HALO", "lib", "jacobi_iterative", "j3d_iterative", "stencil2d",
-           "stencil3d", "last_error"]
+           "stencil3d", "last_error", "cg_csr", "cg_dia", "spmv_csr", "spmv_dia"]
 
 
 def launch_count() -> int:

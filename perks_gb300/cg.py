@@ -1,0 +1,114 @@
+"""Host-side mirror of the reference's CG path.
+
+``cg_csr`` / ``cg_dia`` solve A x = b on the GPU through libperks_gb300.so
+(perks_cg_csr / perks_cg_dia), the replacement for the reference's
+DispatchCG::ProcessDispatchCG (conjugateGradient/cg_dispatcher.cuh:559-916).
+Inputs may be numpy arrays (copied to the device) or CUDA tensors; torch is
+used only to own device memory.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+
+_DT = {"fp64": N.FP64, "fp32": N.FP32, "mixed": N.MIXED}
+
+
+def _dev(a, dtype, device):
+    import torch
+    if isinstance(a, torch.Tensor):
+        return a.to(device=device, dtype=dtype).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device=device, dtype=dtype)
+
+
+def _opts(dtype="fp64", stop="rel", tol=1e-10, max_iter=100000, static_iter=False, kernel="persistent",
+          replace_every=0, ctas=0, stream=None):
+    o = N.CgOpts()
+    N.lib().perks_cg_default_opts(ctypes.byref(o))
+    o.dtype = _DT[dtype]
+    o.stop = {"abs": N.STOP_ABS_RR, "rel": N.STOP_REL}[stop]
+    o.tol = float(tol)
+    o.max_iter = int(max_iter)
+    o.static_iter = int(bool(static_iter))
+    o.kernel = {"persistent": N.KERNEL_PERSISTENT, "per_step": N.KERNEL_PER_STEP}[kernel]
+    o.replace_every = int(replace_every)
+    o.ctas = int(ctas)
+    o.stream = stream
+    return o
+
+
+def _result(r: N.CgResult) -> dict:
+    return {k: getattr(r, k) for k, _ in N.CgResult._fields_}
+
+
+def cg_csr(row_ptr, col, val, b, x0=None, *, dtype="fp64", device="cuda", check=True, **kw):
+    """Solve with CSR A. dtype: 'fp64', 'fp32' (the reference's float build)
+    or 'mixed' (FP32 inner CG, FP64 solution/residual). Returns (x, result)."""
+    import torch
+    vdt = torch.float32 if dtype == "fp32" else torch.float64
+    rp = _dev(row_ptr, torch.int32, device)
+    ci = _dev(col, torch.int32, device)
+    v = _dev(val, vdt, device)
+    bb = _dev(b, vdt, device)
+    n = rp.numel() - 1
+    x = torch.zeros(n, dtype=vdt, device=device) if x0 is None else _dev(x0, vdt, device).clone()
+    if "stream" not in kw:
+        kw["stream"] = ctypes.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
+    o = _opts(dtype, **kw)
+    res = N.CgResult()
+    rc = N.lib().perks_cg_csr(n, ci.numel(), rp.data_ptr(), ci.data_ptr(), v.data_ptr(), bb.data_ptr(),
+                              x.data_ptr(), ctypes.byref(o), ctypes.byref(res))
+    if check:
+        N.check(rc)
+    out = _result(res)
+    out["status"] = rc
+    return x, out
+
+
+def cg_dia(offsets, data, b, x0=None, *, dtype="fp64", device="cuda", check=True, **kw):
+    """Solve with DIA A (offsets[ndiag], data[ndiag][n], diagonal-major)."""
+    import torch
+    vdt = torch.float32 if dtype == "fp32" else torch.float64
+    off = np.ascontiguousarray(offsets, dtype=np.int32)
+    d = _dev(data, vdt, device)
+    bb = _dev(b, vdt, device)
+    n = d.shape[1]
+    x = torch.zeros(n, dtype=vdt, device=device) if x0 is None else _dev(x0, vdt, device).clone()
+    if "stream" not in kw:
+        kw["stream"] = ctypes.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
+    o = _opts(dtype, **kw)
+    res = N.CgResult()
+    rc = N.lib().perks_cg_dia(n, len(off), off.ctypes.data, d.data_ptr(), bb.data_ptr(), x.data_ptr(),
+                              ctypes.byref(o), ctypes.byref(res))
+    if check:
+        N.check(rc)
+    out = _result(res)
+    out["status"] = rc
+    return x, out
+
+
+def spmv_csr(row_ptr, col, val, x, device="cuda"):
+    import torch
+    vdt = torch.float32 if np.dtype(getattr(val, "dtype", np.float64)) == np.float32 else torch.float64
+    rp, ci = _dev(row_ptr, torch.int32, device), _dev(col, torch.int32, device)
+    v, xx = _dev(val, vdt, device), _dev(x, vdt, device)
+    y = torch.empty(rp.numel() - 1, dtype=vdt, device=device)
+    dt = N.FP32 if vdt == torch.float32 else N.FP64
+    N.check(N.lib().perks_spmv_csr(dt, y.numel(), ci.numel(), rp.data_ptr(), ci.data_ptr(), v.data_ptr(),
+                                   xx.data_ptr(), y.data_ptr(), None))
+    return y
+
+
+def spmv_dia(offsets, data, x, device="cuda"):
+    import torch
+    vdt = torch.float32 if np.dtype(getattr(data, "dtype", np.float64)) == np.float32 else torch.float64
+    off = np.ascontiguousarray(offsets, dtype=np.int32)
+    d, xx = _dev(data, vdt, device), _dev(x, vdt, device)
+    y = torch.empty(d.shape[1], dtype=vdt, device=device)
+    dt = N.FP32 if vdt == torch.float32 else N.FP64
+    N.check(N.lib().perks_spmv_dia(dt, y.numel(), len(off), off.ctypes.data, d.data_ptr(), xx.data_ptr(),
+                                   y.data_ptr(), None))
+    return y

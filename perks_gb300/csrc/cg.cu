@@ -1,29 +1,764 @@
-// Conjugate gradient (CSR / DIA): persistent cooperative solver.
+// Conjugate gradient for sm_103a: one persistent cooperative launch per
+// solve (or one launch per phase, as the comparator), CSR or DIA matrices,
+// FP64, FP32 (the reference's float build) or mixed precision.
+//
+// Iteration (cpuConjugateGrad, conjugateGradient/cg_cpu.cpp:40-81, with the
+// stop test of the reference GPU kernel, conjugateGradient/cg_kernels.cuh:834):
+//   p = r (first) or p = r + beta p;  Ap = A p;  alpha = rr / p.Ap;
+//   x += alpha p;  r -= alpha Ap;  rr' = r.r;  beta = rr' / rr
+// Three grid barriers per iteration: after p (the SpMV gathers it), after
+// the p.Ap reduction, after the r.r reduction. Dot products are reduced
+// deterministically: each CTA writes one partial sum, and after the barrier
+// every CTA adds all partials in the same fixed order, so all CTAs derive
+// identical alpha / beta without atomics.
+//
+// Rows are split between CTAs by a merge-path split of rows + nonzeros, so
+// irregular CSR rows are balanced; within a CTA a thread owns a row.
+//
+// Mixed precision (reliable updates, Sleijpen & van der Vorst 1996): the
+// Krylov iteration runs in FP32 (FP32 copy of the matrix values and FP32
+// vectors, dot products accumulated in FP64); the solution is accumulated in
+// FP64 and whenever the FP32 recursive residual has dropped by `delta` since
+// the last update (or claims convergence), x += x_s in FP64 and the true
+// residual r = b - A x is recomputed with the FP64 matrix and re-injected.
+// Convergence is only declared on an FP64 true residual.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include "ptx.cuh"
 #include "runtime.cuh"
+
+namespace perks {
+
+constexpr int kCgThreads = 1024;
+constexpr int kMaxDiag = 32;
+
+struct CgMat {
+  int n, nnz, fmt;        // fmt 0 = CSR, 1 = DIA
+  const int* rp;          // CSR
+  const int* ci;
+  const void* val;        // CSR values or DIA data (dtype of the solve, FP64 for mixed)
+  int ndiag;
+  int off[kMaxDiag];
+};
+
+struct CgParams {
+  CgMat A;
+  const void* b;
+  void* x;                // in: x0, out: solution (FP64 for FP64/mixed, FP32 for FP32)
+  void* r;                // working vectors, working precision
+  void* p[2];             // p, double-buffered between iterations? (single buffer used; see below)
+  void* Ap;
+  // mixed precision extras
+  float* val32;           // FP32 copy of the matrix values (CSR nnz or DIA ndiag*n)
+  double* r64;            // FP64 true residual
+  float* xs;              // FP32 solution increment
+  double* part;           // [4][gridDim] partial sums
+  double tol;
+  int stop, max_iter, static_iter, replace_every;
+  double delta2;          // reliable-update threshold (squared)
+  int* out_iter;          // iterations done
+  int* out_outer;         // reliable updates done
+  double* out_rr;         // final r.r
+  unsigned* bar;
+  unsigned* status;
+};
+
+// Merge-path split: first row of CTA `c` such that row + row_ptr[row] >= c*(n+nnz)/ncta.
+__device__ __forceinline__ int cg_split(const CgMat& A, int c, int ncta) {
+  if (A.fmt != 0) return int((long long)A.n * c / ncta);
+  const long long target = (long long)(A.n + (long long)A.nnz) * c / ncta;
+  int lo = 0, hi = A.n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if ((long long)mid + A.rp[mid] < target) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <class MV, class XV>
+__device__ __forceinline__ double spmv_row(const CgMat& A, const MV* val, const XV* x, int i) {
+  // Accumulates in the working precision of XV (double for FP64, float for FP32).
+  using Acc = XV;
+  Acc acc = Acc(0);
+  if (A.fmt == 0) {
+    const int j0 = A.rp[i], j1 = A.rp[i + 1];
+    for (int j = j0; j < j1; j++) acc = fma(Acc(val[j]), x[A.ci[j]], acc);
+  } else {
+#pragma unroll 4
+    for (int k = 0; k < A.ndiag; k++) {
+      const int c = i + A.off[k];
+      const Acc a = Acc(val[(size_t)k * A.n + i]);
+      if (c >= 0 && c < A.n) acc = fma(a, x[c], acc);
+    }
+  }
+  return double(acc);
+}
+
+// Block-wide sum of two doubles; result valid in every thread.
+__device__ __forceinline__ void block_sum2(double& a, double& b) {
+  __shared__ double sa[32], sb[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  __syncthreads();
+  if (lane == 0) {
+    sa[w] = a;
+    sb[w] = b;
+  }
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  a = lane < nw ? sa[lane] : 0.0;
+  b = lane < nw ? sb[lane] : 0.0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+}
+
+// Grid-wide deterministic sum: every CTA stores its partials, one barrier,
+// then every CTA adds all partials in the same order.
+struct GridSum {
+  double* part;  // [slot][2][gridDim]
+  GridBarrier gb;
+  __device__ bool sum2(int slot, double& a, double& b) {
+    block_sum2(a, b);
+    const int G = gridDim.x;
+    double* ps = part + size_t(slot) * 2 * G;
+    if (threadIdx.x == 0) {
+      ps[blockIdx.x] = a;
+      ps[G + blockIdx.x] = b;
+    }
+    if (!gb.sync()) return false;
+    __shared__ double ra, rb;
+    if (threadIdx.x < 32) {
+      double x = 0.0, y = 0.0;
+      for (int i = threadIdx.x; i < G; i += 32) {
+        x += __ldcg(ps + i);
+        y += __ldcg(ps + G + i);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        x += __shfl_xor_sync(0xffffffffu, x, o);
+        y += __shfl_xor_sync(0xffffffffu, y, o);
+      }
+      if (threadIdx.x == 0) {
+        ra = x;
+        rb = y;
+      }
+    }
+    __syncthreads();
+    a = ra;
+    b = rb;
+    return true;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Plain CG in one precision T (double, or float with the reference's float
+// build rounding of the scalars).
+template <class T>
+__global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_constant__ CgParams P) {
+  const CgMat& A = P.A;
+  const T* val = static_cast<const T*>(A.val);
+  const T* b = static_cast<const T*>(P.b);
+  T* x = static_cast<T*>(P.x);
+  T* r = static_cast<T*>(P.r);
+  T* p = static_cast<T*>(P.p[0]);
+  T* Ap = static_cast<T*>(P.Ap);
+  const int G = gridDim.x;
+  const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
+  GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G)}};
+  const int tid = threadIdx.x, nt = blockDim.x;
+
+  // r = b - A x ; rr = r.r ; bb = b.b
+  double rr = 0.0, bb = 0.0;
+  for (int i = row0 + tid; i < row1; i += nt) {
+    const T ax = T(spmv_row(A, val, x, i));
+    const T ri = T(-1) * ax + b[i];
+    r[i] = ri;
+    rr += double(ri * ri);
+    bb += double(b[i] * b[i]);
+  }
+  if (!gs.sum2(0, rr, bb)) return;
+  T r1 = T(rr);  // float build: r.r rounded to float (cg_cpu.cpp:52)
+  T r0 = T(0);
+  const double tol2 = (P.stop == PERKS_STOP_REL) ? P.tol * P.tol * bb : P.tol * P.tol;
+  const T tol2t = T(P.tol) * T(P.tol);
+  int k = 1;
+  while (true) {
+    if (!P.static_iter) {
+      const bool done = (P.stop == PERKS_STOP_REL) ? (double(r1) < tol2) : (r1 < tol2t);
+      if (done) break;
+    }
+    if (k > P.max_iter) break;
+    if (k > 1) {
+      const T beta = r1 / r0;
+      for (int i = row0 + tid; i < row1; i += nt) p[i] = fma(beta, p[i], r[i]);
+    } else {
+      for (int i = row0 + tid; i < row1; i += nt) p[i] = r[i];
+    }
+    if (!gs.gb.sync()) return;
+    double pap = 0.0, unused = 0.0;
+    for (int i = row0 + tid; i < row1; i += nt) {
+      const T api = T(spmv_row(A, val, p, i));
+      Ap[i] = api;
+      pap += double(p[i] * api);
+    }
+    if (!gs.sum2(1 + (k & 1), pap, unused)) return;
+    const T dot = T(pap);
+    if (!(dot > T(0)) || !isfinite(double(dot))) {
+      if (tid == 0 && blockIdx.x == 0) atomicOr(P.status, kErrBreakdown);
+      return;
+    }
+    const T alpha = r1 / dot;
+    double rrn = 0.0;
+    for (int i = row0 + tid; i < row1; i += nt) {
+      const T pi = p[i];
+      x[i] = fma(alpha, pi, x[i]);
+      const T ri = fma(-alpha, Ap[i], r[i]);
+      r[i] = ri;
+      rrn += double(ri * ri);
+    }
+    if (!gs.sum2(3, rrn, unused)) return;
+    r0 = r1;
+    r1 = T(rrn);
+    k++;
+  }
+  if (blockIdx.x == 0 && tid == 0) {
+    *P.out_iter = k - 1;
+    *P.out_rr = double(r1);
+    *P.out_outer = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision: FP32 Krylov iteration, FP64 solution and true residual.
+__global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant__ CgParams P) {
+  const CgMat& A = P.A;
+  const double* val64 = static_cast<const double*>(A.val);
+  float* val32 = P.val32;
+  const double* b = static_cast<const double*>(P.b);
+  double* x = static_cast<double*>(P.x);
+  double* r64 = P.r64;
+  float* r = static_cast<float*>(P.r);
+  float* p = static_cast<float*>(P.p[0]);
+  float* Ap = static_cast<float*>(P.Ap);
+  float* xs = P.xs;
+  const int G = gridDim.x;
+  const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
+  GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G)}};
+  const int tid = threadIdx.x, nt = blockDim.x;
+
+  // FP32 copy of this CTA's matrix values (CSR nonzeros of its rows, or its
+  // rows of every diagonal).
+  if (A.fmt == 0) {
+    const int j0 = A.rp[row0], j1 = A.rp[row1];
+    for (int j = j0 + tid; j < j1; j += nt) val32[j] = float(val64[j]);
+  } else {
+    for (int k = 0; k < A.ndiag; k++)
+      for (int i = row0 + tid; i < row1; i += nt) val32[(size_t)k * A.n + i] = float(val64[(size_t)k * A.n + i]);
+  }
+  // true residual in FP64
+  double rr = 0.0, bb = 0.0;
+  for (int i = row0 + tid; i < row1; i += nt) {
+    const double ri = b[i] - spmv_row(A, val64, x, i);
+    r64[i] = ri;
+    r[i] = float(ri);
+    xs[i] = 0.0f;
+    rr += ri * ri;
+    bb += b[i] * b[i];
+  }
+  if (!gs.sum2(0, rr, bb)) return;
+  const double tol2 = (P.stop == PERKS_STOP_REL) ? P.tol * P.tol * bb : P.tol * P.tol;
+  double maxrr = rr, rr0 = 0.0;
+  int k = 1, outer = 0, since = 0;
+  while (true) {
+    if (!P.static_iter && rr < tol2) break;
+    if (k > P.max_iter) break;
+    if (k > 1) {
+      const float beta = float(rr / rr0);
+      for (int i = row0 + tid; i < row1; i += nt) p[i] = fmaf(beta, p[i], r[i]);
+    } else {
+      for (int i = row0 + tid; i < row1; i += nt) p[i] = r[i];
+    }
+    if (!gs.gb.sync()) return;
+    double pap = 0.0, unused = 0.0;
+    for (int i = row0 + tid; i < row1; i += nt) {
+      const float api = float(spmv_row(A, val32, p, i));
+      Ap[i] = api;
+      pap += double(p[i]) * double(api);
+    }
+    if (!gs.sum2(1 + (k & 1), pap, unused)) return;
+    if (!(pap > 0.0) || !isfinite(pap)) {
+      if (tid == 0 && blockIdx.x == 0) atomicOr(P.status, kErrBreakdown);
+      return;
+    }
+    const float alpha = float(rr / pap);
+    double rrn = 0.0;
+    for (int i = row0 + tid; i < row1; i += nt) {
+      xs[i] = fmaf(alpha, p[i], xs[i]);
+      const float ri = fmaf(-alpha, Ap[i], r[i]);
+      r[i] = ri;
+      rrn += double(ri) * double(ri);
+    }
+    if (!gs.sum2(3, rrn, unused)) return;
+    since++;
+    const bool update = rrn < P.delta2 * maxrr || rrn < tol2 || (P.replace_every > 0 && since >= P.replace_every) ||
+                        k == P.max_iter;
+    if (update) {
+      // x += xs in FP64; true residual with the FP64 matrix
+      for (int i = row0 + tid; i < row1; i += nt) {
+        x[i] += double(xs[i]);
+        xs[i] = 0.0f;
+      }
+      if (!gs.gb.sync()) return;
+      double rt = 0.0, un2 = 0.0;
+      for (int i = row0 + tid; i < row1; i += nt) {
+        const double ri = b[i] - spmv_row(A, val64, x, i);
+        r64[i] = ri;
+        r[i] = float(ri);
+        rt += ri * ri;
+      }
+      if (!gs.sum2(0, rt, un2)) return;
+      rrn = rt;
+      maxrr = rt;
+      outer++;
+      since = 0;
+    }
+    rr0 = rr;
+    rr = rrn;
+    k++;
+  }
+  if (blockIdx.x == 0 && tid == 0) {
+    *P.out_iter = k - 1;
+    *P.out_rr = rr;
+    *P.out_outer = outer;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// One-launch-per-phase comparator kernels (plain CG, FP64 or FP32). Scalars
+// live on the device: s[0] = r1 (r.r), s[1] = r0, s[2] = p.Ap, s[3] = bb,
+// s[4] = done flag, s[5] = iterations.
+template <class T>
+__global__ void cg_phase_init(const __grid_constant__ CgParams P, double* part) {
+  const CgMat& A = P.A;
+  const T* val = static_cast<const T*>(A.val);
+  const T* b = static_cast<const T*>(P.b);
+  const T* x = static_cast<const T*>(P.x);
+  T* r = static_cast<T*>(P.r);
+  double rr = 0.0, bb = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+    const T ri = T(-1) * T(spmv_row(A, val, x, i)) + b[i];
+    r[i] = ri;
+    rr += double(ri * ri);
+    bb += double(b[i] * b[i]);
+  }
+  block_sum2(rr, bb);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = rr;
+    part[gridDim.x + blockIdx.x] = bb;
+  }
+}
+
+// Reduce the partials of the previous kernel into scalar slot `which`
+// (0: r.r at init, 2: p.Ap, 1: new r.r) and update the iteration state.
+template <class T>
+__global__ void cg_phase_reduce(const __grid_constant__ CgParams P, double* part, int nparts, double* s, int which) {
+  double a = 0.0, bsum = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+    a += part[i];
+    bsum += part[nparts + i];
+  }
+  block_sum2(a, bsum);
+  if (threadIdx.x != 0) return;
+  if (which != 0 && s[4] != 0.0) return;  // converged or broken down: keep the final state
+  if (which == 0) {
+    s[0] = double(T(a));
+    s[3] = bsum;
+    s[5] = 0.0;
+  } else if (which == 2) {
+    s[2] = double(T(a));
+    if (!(s[2] > 0.0)) {
+      s[4] = 1.0;
+      atomicOr(P.status, kErrBreakdown);
+    }
+  } else {
+    s[1] = s[0];
+    s[0] = double(T(a));
+    s[5] += 1.0;
+  }
+  if (which != 2) {
+    const double tol2 = (P.stop == PERKS_STOP_REL) ? P.tol * P.tol * s[3] : double(T(P.tol) * T(P.tol));
+    if ((!P.static_iter && s[0] < tol2) || s[5] >= P.max_iter) s[4] = 1.0;
+  }
+}
+
+template <class T>
+__global__ void cg_phase_p(const __grid_constant__ CgParams P, const double* s) {
+  if (s[4] != 0.0) return;
+  T* p = static_cast<T*>(P.p[0]);
+  const T* r = static_cast<const T*>(P.r);
+  const bool first = s[5] == 0.0;
+  const T beta = first ? T(0) : T(s[0]) / T(s[1]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.A.n; i += gridDim.x * blockDim.x)
+    p[i] = first ? r[i] : fma(beta, p[i], r[i]);
+}
+
+template <class T>
+__global__ void cg_phase_spmv(const __grid_constant__ CgParams P, const double* s, double* part) {
+  if (s[4] != 0.0) return;
+  const T* val = static_cast<const T*>(P.A.val);
+  const T* p = static_cast<const T*>(P.p[0]);
+  T* Ap = static_cast<T*>(P.Ap);
+  double pap = 0.0, u = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.A.n; i += gridDim.x * blockDim.x) {
+    const T api = T(spmv_row(P.A, val, p, i));
+    Ap[i] = api;
+    pap += double(p[i] * api);
+  }
+  block_sum2(pap, u);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = pap;
+    part[gridDim.x + blockIdx.x] = 0.0;
+  }
+}
+
+template <class T>
+__global__ void cg_phase_update(const __grid_constant__ CgParams P, const double* s, double* part) {
+  if (s[4] != 0.0) return;
+  T* x = static_cast<T*>(P.x);
+  T* r = static_cast<T*>(P.r);
+  const T* p = static_cast<const T*>(P.p[0]);
+  const T* Ap = static_cast<const T*>(P.Ap);
+  const T alpha = T(s[0]) / T(s[2]);
+  double rr = 0.0, u = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.A.n; i += gridDim.x * blockDim.x) {
+    x[i] = fma(alpha, p[i], x[i]);
+    const T ri = fma(-alpha, Ap[i], r[i]);
+    r[i] = ri;
+    rr += double(ri * ri);
+  }
+  block_sum2(rr, u);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = rr;
+    part[gridDim.x + blockIdx.x] = 0.0;
+  }
+}
+
+// True relative residual ||b - A x|| / ||b|| in FP64 (reported, not used for stopping).
+template <class T>
+__global__ void cg_true_residual(CgMat A, const void* bv, const void* xv, double* part) {
+  const T* val = static_cast<const T*>(A.val);
+  const T* b = static_cast<const T*>(bv);
+  const T* x = static_cast<const T*>(xv);
+  double rr = 0.0, bb = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    if (A.fmt == 0) {
+      for (int j = A.rp[i]; j < A.rp[i + 1]; j++) acc = fma(double(val[j]), double(x[A.ci[j]]), acc);
+    } else {
+      for (int k = 0; k < A.ndiag; k++) {
+        const int c = i + A.off[k];
+        if (c >= 0 && c < A.n) acc = fma(double(val[(size_t)k * A.n + i]), double(x[c]), acc);
+      }
+    }
+    const double ri = double(b[i]) - acc;
+    rr += ri * ri;
+    bb += double(b[i]) * double(b[i]);
+  }
+  block_sum2(rr, bb);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = rr;
+    part[gridDim.x + blockIdx.x] = bb;
+  }
+}
+
+__global__ void sum_partials(const double* part, int n, double* out) {
+  double a = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    a += part[i];
+    b += part[n + i];
+  }
+  block_sum2(a, b);
+  if (threadIdx.x == 0) {
+    out[0] = a;
+    out[1] = b;
+  }
+}
+
+template <class T>
+__global__ void spmv_kernel(CgMat A, const T* x, T* y) {
+  const T* val = static_cast<const T*>(A.val);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x)
+    y[i] = T(spmv_row(A, val, x, i));
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, perks_cg_result* res) {
+  if (!o) return fail(PERKS_ERR_INVALID_ARG, "opts is NULL");
+  if (o->dtype != PERKS_FP64 && o->dtype != PERKS_FP32 && o->dtype != PERKS_MIXED)
+    return fail(PERKS_ERR_INVALID_ARG, "unknown CG dtype");
+  if (o->stop != PERKS_STOP_ABS_RR && o->stop != PERKS_STOP_REL) return fail(PERKS_ERR_INVALID_ARG, "unknown stop rule");
+  if (o->max_iter < 0 || !(o->tol >= 0)) return fail(PERKS_ERR_INVALID_ARG, "bad max_iter or tol");
+  if (o->kernel != PERKS_KERNEL_PERSISTENT && o->kernel != PERKS_KERNEL_PER_STEP)
+    return fail(PERKS_ERR_INVALID_ARG, "unknown kernel kind");
+  if (o->dtype == PERKS_MIXED && o->kernel != PERKS_KERNEL_PERSISTENT)
+    return fail(PERKS_ERR_UNSUPPORTED, "mixed precision runs in the persistent kernel only");
+  const DeviceInfo* dev = device_info();
+  if (!dev) return PERKS_ERR_NO_DEVICE;
+  cudaStream_t s = static_cast<cudaStream_t>(o->stream);
+  const int n = A.n;
+  const bool f32 = o->dtype == PERKS_FP32;
+  const size_t ws = f32 || o->dtype == PERKS_MIXED ? 4 : 8;  // working precision bytes
+  int st = PERKS_OK;
+  const int ctas = o->ctas > 0 ? std::min(o->ctas, dev->sms) : dev->sms;
+  const size_t vbytes = (size_t(n) * ws + 255) & ~size_t(255);
+  const size_t v64 = (size_t(n) * 8 + 255) & ~size_t(255);
+  const size_t nval = A.fmt == 0 ? size_t(A.nnz) : size_t(A.ndiag) * n;
+  constexpr size_t kTail = 80 * 1024;   // partial sums (4 slots x 2 x 1024 CTAs) + scalars
+  size_t need = 3 * vbytes + kTail;     // r, p, Ap + tail
+  if (o->dtype == PERKS_MIXED) need += v64 + vbytes + ((nval * 4 + 255) & ~size_t(255));
+  unsigned char* w = static_cast<unsigned char*>(workspace(kWsCgVec, need, &st));
+  if (!w) return st;
+  SyncWords sw;
+  if ((st = sync_words(&sw, s)) != PERKS_OK) return st;
+  CgParams P{};
+  P.A = A;
+  P.b = b;
+  P.x = x;
+  P.r = w;
+  P.p[0] = w + vbytes;
+  P.p[1] = P.p[0];
+  P.Ap = w + 2 * vbytes;
+  unsigned char* tail = w + 3 * vbytes;
+  P.part = reinterpret_cast<double*>(tail);          // 4 slots x 2 x (<= 1024 CTAs)
+  double* scal = P.part + 8 * 1024;                    // device scalars / results (32 doubles)
+  unsigned char* more = tail + kTail;
+  if (o->dtype == PERKS_MIXED) {
+    P.r64 = reinterpret_cast<double*>(more);
+    P.xs = reinterpret_cast<float*>(more + v64);
+    P.val32 = reinterpret_cast<float*>(more + v64 + vbytes);
+  }
+  P.tol = o->tol;
+  P.stop = o->stop;
+  P.max_iter = o->max_iter;
+  P.static_iter = o->static_iter;
+  P.replace_every = o->replace_every;
+  P.delta2 = 0.1 * 0.1;
+  P.out_iter = reinterpret_cast<int*>(scal + 16);
+  P.out_outer = reinterpret_cast<int*>(scal + 17);
+  P.out_rr = scal + 18;
+  P.bar = sw.bar;
+  P.status = sw.status;
+  PERKS_CUDA(cudaMemsetAsync(scal, 0, 32 * sizeof(double), s));
+
+  cudaEvent_t e0, e1;
+  PERKS_CUDA(cudaEventCreate(&e0));
+  PERKS_CUDA(cudaEventCreate(&e1));
+  PERKS_CUDA(cudaEventRecord(e0, s));
+  int launches = 0;
+  if (o->kernel == PERKS_KERNEL_PERSISTENT) {
+    const void* kern = o->dtype == PERKS_MIXED ? (const void*)cg_mixed
+                       : f32                   ? (const void*)cg_persistent<float>
+                                               : (const void*)cg_persistent<double>;
+    int per_sm = 0;
+    PERKS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCgThreads, 0));
+    if (per_sm < 1) return fail(PERKS_ERR_LAUNCH, "CG kernel does not fit on an SM");
+    void* args[] = {&P};
+    cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(ctas), dim3(kCgThreads), args, 0, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchCooperativeKernel(cg)");
+    launches = 1;
+  } else {
+    // one launch per phase; scalars on the device; the host checks the
+    // convergence flag every `chunk` iterations
+    double* sv = scal;  // s[0..5]
+    const int grid = dev->sms * 2, bt = 512;
+    double* part = P.part;
+    if (f32) {
+      cg_phase_init<float><<<grid, bt, 0, s>>>(P, part);
+      cg_phase_reduce<float><<<1, 1024, 0, s>>>(P, part, grid, sv, 0);
+    } else {
+      cg_phase_init<double><<<grid, bt, 0, s>>>(P, part);
+      cg_phase_reduce<double><<<1, 1024, 0, s>>>(P, part, grid, sv, 0);
+    }
+    launches = 2;
+    const int chunk = 32;
+    double flag = 0.0;
+    for (int it = 0; it < o->max_iter + 1 && flag == 0.0; it += chunk) {
+      for (int c = 0; c < chunk; c++) {
+        if (f32) {
+          cg_phase_p<float><<<grid, bt, 0, s>>>(P, sv);
+          cg_phase_spmv<float><<<grid, bt, 0, s>>>(P, sv, part);
+          cg_phase_reduce<float><<<1, 1024, 0, s>>>(P, part, grid, sv, 2);
+          cg_phase_update<float><<<grid, bt, 0, s>>>(P, sv, part);
+          cg_phase_reduce<float><<<1, 1024, 0, s>>>(P, part, grid, sv, 1);
+        } else {
+          cg_phase_p<double><<<grid, bt, 0, s>>>(P, sv);
+          cg_phase_spmv<double><<<grid, bt, 0, s>>>(P, sv, part);
+          cg_phase_reduce<double><<<1, 1024, 0, s>>>(P, part, grid, sv, 2);
+          cg_phase_update<double><<<grid, bt, 0, s>>>(P, sv, part);
+          cg_phase_reduce<double><<<1, 1024, 0, s>>>(P, part, grid, sv, 1);
+        }
+        launches += 5;
+      }
+      PERKS_CUDA(cudaMemcpyAsync(&flag, sv + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
+      PERKS_CUDA(cudaStreamSynchronize(s));
+    }
+    PERKS_CUDA(cudaGetLastError());
+  }
+  PERKS_CUDA(cudaEventRecord(e1, s));
+  count_launch(launches);
+  int rc = check_status(sw, s);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != PERKS_OK) return rc;
+  // results
+  double hs[24] = {0};
+  PERKS_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, s));
+  PERKS_CUDA(cudaStreamSynchronize(s));
+  int iters = 0, outer = 0;
+  double rr = 0.0;
+  if (o->kernel == PERKS_KERNEL_PERSISTENT) {
+    std::memcpy(&iters, &hs[16], sizeof(int));
+    std::memcpy(&outer, &hs[17], sizeof(int));
+    rr = hs[18];
+  } else {
+    iters = int(hs[5]);
+    rr = hs[0];
+  }
+  // true relative residual in FP64
+  double* tpart = P.part;
+  const int tg = dev->sms * 2;
+  const bool val_f32 = f32;
+  if (val_f32) cg_true_residual<float><<<tg, 512, 0, s>>>(A, b, x, tpart);
+  else cg_true_residual<double><<<tg, 512, 0, s>>>(A, b, x, tpart);
+  sum_partials<<<1, 1024, 0, s>>>(tpart, tg, scal + 20);
+  count_launch(2);
+  double tr[2];
+  PERKS_CUDA(cudaMemcpyAsync(tr, scal + 20, sizeof(tr), cudaMemcpyDeviceToHost, s));
+  PERKS_CUDA(cudaStreamSynchronize(s));
+  if (res) {
+    res->iterations = iters;
+    res->outer = outer;
+    res->rr = rr;
+    res->true_rel_res = tr[1] > 0 ? std::sqrt(tr[0] / tr[1]) : std::sqrt(tr[0]);
+    res->ms = ms;
+    res->launches = launches;
+  }
+  const double thr = o->stop == PERKS_STOP_REL ? o->tol * o->tol * tr[1] : o->tol * o->tol;
+  if (!o->static_iter && iters >= o->max_iter && !(rr < thr))
+    return fail(PERKS_ERR_NOT_CONVERGED, "CG reached max_iter=" + std::to_string(o->max_iter) +
+                                             " (r.r = " + std::to_string(rr) + ")");
+  return PERKS_OK;
+}
+
+}  // namespace perks
 
 using namespace perks;
 
 extern "C" {
+
 void perks_cg_default_opts(perks_cg_opts* o) {
   if (!o) return;
   *o = perks_cg_opts{};
   o->dtype = PERKS_FP64;
   o->stop = PERKS_STOP_REL;
   o->tol = 1e-10;
-  o->max_iter = 10000;
+  o->max_iter = 100000;
+  o->static_iter = 0;
   o->kernel = PERKS_KERNEL_PERSISTENT;
+  o->replace_every = 0;
+  o->ctas = 0;
+  o->stream = nullptr;
 }
-int perks_cg_csr(int, int, const int*, const int*, const void*, const void*, void*, const perks_cg_opts*,
-                 perks_cg_result*) {
-  return fail(PERKS_ERR_UNSUPPORTED, "CG not built yet");
+
+int perks_cg_csr(int n, int nnz, const int* rp, const int* ci, const void* val, const void* b, void* x,
+                 const perks_cg_opts* o, perks_cg_result* res) {
+  if (n <= 0 || nnz < 0 || !rp || !ci || !val || !b || !x) return fail(PERKS_ERR_INVALID_ARG, "bad CSR arguments");
+  CgMat A{};
+  A.n = n;
+  A.nnz = nnz;
+  A.fmt = 0;
+  A.rp = rp;
+  A.ci = ci;
+  A.val = val;
+  return cg_solve(A, b, x, o, res);
 }
-int perks_cg_dia(int, int, const int*, const void*, const void*, void*, const perks_cg_opts*, perks_cg_result*) {
-  return fail(PERKS_ERR_UNSUPPORTED, "CG not built yet");
+
+int perks_cg_dia(int n, int ndiag, const int* off, const void* data, const void* b, void* x, const perks_cg_opts* o,
+                 perks_cg_result* res) {
+  if (n <= 0 || ndiag <= 0 || ndiag > kMaxDiag || !off || !data || !b || !x)
+    return fail(PERKS_ERR_INVALID_ARG, "bad DIA arguments (at most 32 diagonals)");
+  CgMat A{};
+  A.n = n;
+  A.fmt = 1;
+  A.ndiag = ndiag;
+  for (int k = 0; k < ndiag; k++) {
+    if (off[k] <= -n || off[k] >= n) return fail(PERKS_ERR_INVALID_ARG, "DIA offset out of range");
+    A.off[k] = off[k];
+  }
+  A.val = data;
+  return cg_solve(A, b, x, o, res);
 }
-int perks_spmv_csr(int, int, int, const int*, const int*, const void*, const void*, void*, void*) {
-  return fail(PERKS_ERR_UNSUPPORTED, "SpMV not built yet");
+
+int perks_spmv_csr(int dtype, int n, int nnz, const int* rp, const int* ci, const void* val, const void* x, void* y,
+                   void* stream) {
+  if (n <= 0 || !rp || !ci || !val || !x || !y) return fail(PERKS_ERR_INVALID_ARG, "bad CSR arguments");
+  if (dtype != PERKS_FP32 && dtype != PERKS_FP64) return fail(PERKS_ERR_INVALID_ARG, "dtype");
+  const DeviceInfo* dev = device_info();
+  if (!dev) return PERKS_ERR_NO_DEVICE;
+  CgMat A{};
+  A.n = n;
+  A.nnz = nnz;
+  A.fmt = 0;
+  A.rp = rp;
+  A.ci = ci;
+  A.val = val;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (dtype == PERKS_FP32)
+    spmv_kernel<float><<<dev->sms * 4, 256, 0, s>>>(A, static_cast<const float*>(x), static_cast<float*>(y));
+  else
+    spmv_kernel<double><<<dev->sms * 4, 256, 0, s>>>(A, static_cast<const double*>(x), static_cast<double*>(y));
+  count_launch(1);
+  PERKS_CUDA(cudaGetLastError());
+  PERKS_CUDA(cudaStreamSynchronize(s));
+  return PERKS_OK;
 }
-int perks_spmv_dia(int, int, int, const int*, const void*, const void*, void*, void*) {
-  return fail(PERKS_ERR_UNSUPPORTED, "SpMV not built yet");
+
+int perks_spmv_dia(int dtype, int n, int ndiag, const int* off, const void* data, const void* x, void* y,
+                   void* stream) {
+  if (n <= 0 || ndiag <= 0 || ndiag > kMaxDiag || !off || !data || !x || !y)
+    return fail(PERKS_ERR_INVALID_ARG, "bad DIA arguments");
+  if (dtype != PERKS_FP32 && dtype != PERKS_FP64) return fail(PERKS_ERR_INVALID_ARG, "dtype");
+  const DeviceInfo* dev = device_info();
+  if (!dev) return PERKS_ERR_NO_DEVICE;
+  CgMat A{};
+  A.n = n;
+  A.fmt = 1;
+  A.ndiag = ndiag;
+  for (int k = 0; k < ndiag; k++) A.off[k] = off[k];
+  A.val = data;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (dtype == PERKS_FP32)
+    spmv_kernel<float><<<dev->sms * 4, 256, 0, s>>>(A, static_cast<const float*>(x), static_cast<float*>(y));
+  else
+    spmv_kernel<double><<<dev->sms * 4, 256, 0, s>>>(A, static_cast<const double*>(x), static_cast<double*>(y));
+  count_launch(1);
+  PERKS_CUDA(cudaGetLastError());
+  PERKS_CUDA(cudaStreamSynchronize(s));
+  return PERKS_OK;
 }
-}
+
+}  // extern "C"

@@ -1,0 +1,119 @@
+"""GPU parity of the CG path through the C ABI against the oracle (CPU
+restatement of the reference's CG, conjugateGradient/cg_cpu.cpp:40-81).
+
+CG on the GPU reduces dot products in a different order than the sequential
+CPU loop, so results are not bit-identical; the bar is the benchmark spec's:
+the same iteration count (within 1, or 1% for long solves) and a true
+relative residual ||b - A x|| / ||b|| <= 1e-10 recomputed in FP64."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def true_rel(rp, ci, v, b, x):
+    from oracle import oracle as O
+    r = b - O.spmv_csr(rp, ci, np.asarray(v, np.float64), np.asarray(x, np.float64))
+    return np.linalg.norm(r) / np.linalg.norm(b)
+
+
+def it_close(a, b):
+    return abs(a - b) <= max(1, int(0.01 * max(a, b)))
+
+
+@pytest.mark.parametrize("kernel", ["persistent", "per_step"])
+@pytest.mark.parametrize("matrix", ["lap2d", "lap3d", "spd"])
+def test_cg_fp64_csr_vs_oracle(native, cuda, oracle, kernel, matrix):
+    from perks_gb300 import matrices as M
+    rp, ci, v = {"lap2d": lambda: M.laplacian_2d(96), "lap3d": lambda: M.laplacian_3d(24),
+                 "spd": lambda: M.random_spd(20000, 3)}[matrix]()
+    b = np.random.default_rng(1).uniform(-1, 1, len(rp) - 1)
+    xo, it, _, _ = oracle.cg(rp, ci, v, b, max_iter=20000, stop=1, tol=1e-10)
+    x, res = native.cg_csr(rp, ci, v, b, dtype="fp64", tol=1e-10, kernel=kernel, device=cuda)
+    assert it_close(res["iterations"], it), (res, it)
+    assert res["true_rel_res"] <= 1e-10 * 1.05
+    assert true_rel(rp, ci, v, b, x.cpu().numpy()) <= 1e-10 * 1.05
+    assert np.allclose(x.cpu().numpy(), xo, rtol=1e-7, atol=1e-9)
+
+
+def test_cg_dia_matches_csr(native, cuda, oracle):
+    from perks_gb300 import matrices as M
+    rp, ci, v = M.laplacian_2d(80)
+    off, data = M.csr_to_dia(rp, ci, v)
+    b = np.random.default_rng(2).uniform(-1, 1, len(rp) - 1)
+    xo, it, _ = oracle.cg_dia(off, data, b, max_iter=20000, stop=1, tol=1e-10)
+    x, res = native.cg_dia(off, data, b, dtype="fp64", tol=1e-10, device=cuda)
+    assert it_close(res["iterations"], it)
+    assert true_rel(rp, ci, v, b, x.cpu().numpy()) <= 1e-10 * 1.05
+
+
+def test_cg_reference_mode_tridiag(native, cuda, oracle):
+    """The reference's own setting: genTridiag matrix, rhs = 1, x0 = 0, stop on
+    absolute r.r < tol^2 (conjugateGradient/cg_driver.cu:140-210)."""
+    for n in (1000, 100000):
+        rp, ci, v = oracle.gen_tridiag(n, 1, np.float64)
+        b = np.ones(n)
+        xo, it, rr, _ = oracle.cg(rp, ci, v, b, max_iter=n, stop=0, tol=1e-10)
+        x, res = native.cg_csr(rp, ci, v, b, dtype="fp64", stop="abs", tol=1e-10, max_iter=n, device=cuda)
+        assert it_close(res["iterations"], it), (n, res, it)
+        assert res["rr"] < 1e-20
+        assert np.allclose(x.cpu().numpy(), xo, rtol=1e-8, atol=1e-10)
+
+
+def test_cg_float_build_tracks_oracle(native, cuda, oracle):
+    """FP32 (the reference's float build): a few iterations agree with the
+    float oracle to float rounding."""
+    rp, ci, v = oracle.gen_tridiag(5000, 2, np.float32)
+    b = np.ones(5000, np.float32)
+    xo, it, _, tr = oracle.cg(rp, ci, v, b, max_iter=6, static_iter=True, trace=True)
+    x, res = native.cg_csr(rp, ci, v, b, dtype="fp32", max_iter=6, static_iter=True, device=cuda)
+    assert res["iterations"] == 6
+    assert np.allclose(x.cpu().numpy(), xo, rtol=1e-4, atol=1e-6)
+
+
+@pytest.mark.parametrize("matrix", ["lap2d", "spd"])
+@pytest.mark.parametrize("fmt", ["csr", "dia"])
+def test_cg_mixed_reaches_fp64_accuracy(native, cuda, oracle, matrix, fmt):
+    from perks_gb300 import matrices as M
+    if matrix == "spd" and fmt == "dia":
+        pytest.skip("random pattern has too many diagonals for DIA")
+    rp, ci, v = M.laplacian_2d(128) if matrix == "lap2d" else M.random_spd(50000, 4)
+    b = np.random.default_rng(3).uniform(-1, 1, len(rp) - 1)
+    _, it64, _, _ = oracle.cg(rp, ci, v, b, max_iter=50000, stop=1, tol=1e-10)
+    if fmt == "csr":
+        x, res = native.cg_csr(rp, ci, v, b, dtype="mixed", tol=1e-10, device=cuda)
+    else:
+        off, data = M.csr_to_dia(rp, ci, v)
+        x, res = native.cg_dia(off, data, b, dtype="mixed", tol=1e-10, device=cuda)
+    assert true_rel(rp, ci, v, b, x.cpu().numpy()) <= 1e-10 * 1.05
+    assert res["outer"] >= 1
+    assert res["iterations"] <= 2 * it64 + 50, (res, it64)
+
+
+def test_cg_breakdown_reported(native, cuda):
+    from perks_gb300 import matrices as M
+    rp, ci, v = M.laplacian_2d(16)
+    b = np.ones(len(rp) - 1)
+    x, res = native.cg_csr(rp, ci, -v, b, dtype="fp64", device=cuda, check=False)
+    assert res["status"] == -17
+
+
+def test_cg_not_converged_reported(native, cuda):
+    from perks_gb300 import matrices as M
+    rp, ci, v = M.laplacian_2d(64)
+    b = np.ones(len(rp) - 1)
+    x, res = native.cg_csr(rp, ci, v, b, dtype="fp64", max_iter=5, device=cuda, check=False)
+    assert res["status"] == -18 and res["iterations"] == 5
+
+
+def test_spmv_matches_oracle(native, cuda, oracle):
+    from perks_gb300 import matrices as M
+    rp, ci, v = M.random_spd(30000, 5)
+    x = np.random.default_rng(4).standard_normal(len(rp) - 1)
+    y = native.spmv_csr(rp, ci, v, x, device=cuda).cpu().numpy()
+    assert np.allclose(y, oracle.spmv_csr(rp, ci, v, x), rtol=1e-13, atol=1e-12)
+    rp, ci, v = M.laplacian_3d(20)
+    off, data = M.csr_to_dia(rp, ci, v)
+    x = np.random.default_rng(5).standard_normal(len(rp) - 1)
+    y = native.spmv_dia(off, data, x, device=cuda).cpu().numpy()
+    assert np.allclose(y, oracle.spmv_dia(off, data, x), rtol=1e-13, atol=1e-12)
