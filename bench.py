@@ -177,6 +177,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extra", action="store_true", help="skip the comparator measurements")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="profiling mode: one warm-up call, then one call of the headline kernel with this many "
+                         "time steps, then exit (for ncu captures of a short launch)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if ws > 1:
@@ -206,6 +209,14 @@ def main():
     d_in = host.to(dev)
     d_out = torch.empty_like(d_in)
     kw = dict(kernel="persistent", order="reference", l2_sweep=False)
+    if args.profile_steps > 0:
+        P.stencil2d(d_in, SHAPE, 2, out=d_out, **kw)
+        torch.cuda.synchronize()
+        _, st = P.stencil2d(d_in, SHAPE, args.profile_steps, out=d_out, **kw)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_steps": args.profile_steps, "kernel_ms": st["ms"],
+                          "gcells_per_s": st["gcells_per_s"]}), flush=True)
+        return
 
     def step():
         _, st = P.stencil2d(d_in, SHAPE, TSTEPS, out=d_out, **kw)
@@ -284,6 +295,8 @@ def main():
         extra["persistent_fast_fp64_gcells"] = round(st["gcells_per_s"], 2)
         del d64, o64
         extra["cached_fraction"] = round(kernel_cached_fraction(P, d_in, d_out), 4)
+        extra.update(extra_3d(P, torch))
+        extra.update(extra_cg(P, torch))
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -309,6 +322,43 @@ def main():
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def extra_3d(P, torch):
+    """3D shapes of the stencil sweep at 512^3 (FP32 and FP64, 20 steps each)."""
+    out = {}
+    for dt, tag in ((torch.float32, "fp32"), (torch.float64, "fp64")):
+        d = torch.rand((512, 512, 512), dtype=dt, device="cuda")
+        o = torch.empty_like(d)
+        for shape in ("3d7pt", "3d27pt"):
+            P.stencil3d(d, shape, 2, out=o, order="fast")
+            for order in ("reference", "fast"):
+                _, st = P.stencil3d(d, shape, 20, out=o, order=order)
+                out[f"{shape}_512_{tag}_{order}_gcells"] = round(st["gcells_per_s"], 2)
+        del d, o
+    return out
+
+
+def extra_cg(P, torch):
+    """CG time to a 1e-10 relative residual on the 2D 5-point Laplacian,
+    2048^2 (4.19M rows, 20.96M nonzeros), RHS uniform [-1,1) seed 1, x0 = 0:
+    FP64 vs mixed precision (FP32 inner, FP64 reliable updates), CSR and DIA."""
+    import numpy as np
+    from perks_gb300 import matrices as M
+    rp, ci, v = M.laplacian_2d(2048)
+    b = np.random.default_rng(1).uniform(-1, 1, len(rp) - 1)
+    off, data = M.csr_to_dia(rp, ci, v)
+    out = {}
+    for fmt in ("csr", "dia"):
+        for dt in ("fp64", "mixed"):
+            if fmt == "csr":
+                x, res = P.cg_csr(rp, ci, v, b, dtype=dt, tol=1e-10)
+            else:
+                x, res = P.cg_dia(off, data, b, dtype=dt, tol=1e-10)
+            out[f"cg_lap2d_2048_{fmt}_{dt}"] = {"ms": round(res["ms"], 2), "iterations": res["iterations"],
+                                                "us_per_iter": round(1e3 * res["ms"] / max(1, res["iterations"]), 2),
+                                                "true_rel_res": res["true_rel_res"]}
+    return out
 
 
 def kernel_cached_fraction(P, d_in, d_out):

@@ -80,22 +80,32 @@ __device__ __forceinline__ int cg_split(const CgMat& A, int c, int ncta) {
 }
 
 template <class MV, class XV>
-__device__ __forceinline__ double spmv_row(const CgMat& A, const MV* val, const XV* x, int i) {
-  // Accumulates in the working precision of XV (double for FP64, float for FP32).
-  using Acc = XV;
-  Acc acc = Acc(0);
+__device__ __forceinline__ XV spmv_row(const CgMat& A, const MV* __restrict__ val, const XV* __restrict__ x, int i) {
+  // Accumulates in the working precision XV (double for FP64, float for FP32).
+  XV acc = XV(0);
   if (A.fmt == 0) {
-    const int j0 = A.rp[i], j1 = A.rp[i + 1];
-    for (int j = j0; j < j1; j++) acc = fma(Acc(val[j]), x[A.ci[j]], acc);
+    const int j0 = __ldg(A.rp + i), j1 = __ldg(A.rp + i + 1);
+    int j = j0;
+    // four independent gathers in flight per row
+    for (; j + 4 <= j1; j += 4) {
+      const int c0 = __ldg(A.ci + j), c1 = __ldg(A.ci + j + 1), c2 = __ldg(A.ci + j + 2), c3 = __ldg(A.ci + j + 3);
+      const XV v0 = XV(__ldg(val + j)), v1 = XV(__ldg(val + j + 1)), v2 = XV(__ldg(val + j + 2)), v3 = XV(__ldg(val + j + 3));
+      const XV x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
+      acc = fma(v0, x0, acc);
+      acc = fma(v1, x1, acc);
+      acc = fma(v2, x2, acc);
+      acc = fma(v3, x3, acc);
+    }
+    for (; j < j1; j++) acc = fma(XV(__ldg(val + j)), x[__ldg(A.ci + j)], acc);
   } else {
-#pragma unroll 4
+#pragma unroll 8
     for (int k = 0; k < A.ndiag; k++) {
       const int c = i + A.off[k];
-      const Acc a = Acc(val[(size_t)k * A.n + i]);
+      const XV a = XV(__ldg(val + (size_t)k * A.n + i));
       if (c >= 0 && c < A.n) acc = fma(a, x[c], acc);
     }
   }
-  return double(acc);
+  return acc;
 }
 
 // Block-wide sum of two doubles; result valid in every thread.
@@ -162,31 +172,44 @@ struct GridSum {
 };
 
 // ---------------------------------------------------------------------------
+// Row loops: each thread takes kU rows per pass (rows i, i+nt, ..., so warps
+// stay coalesced) and issues all of their loads before any use.
+constexpr int kU = 4;
+#define CG_ROWS(i, BODY)                                                   \
+  for (int base_ = row0 + tid; base_ < row1; base_ += nt * kU) {           \
+    _Pragma("unroll") for (int u_ = 0; u_ < kU; u_++) {                    \
+      const int i = base_ + u_ * nt;                                       \
+      if (i < row1) { BODY }                                               \
+    }                                                                      \
+  }
+
 // Plain CG in one precision T (double, or float with the reference's float
-// build rounding of the scalars).
+// build rounding of the scalars r.r, p.Ap, alpha and beta).
 template <class T>
 __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_constant__ CgParams P) {
   const CgMat& A = P.A;
-  const T* val = static_cast<const T*>(A.val);
-  const T* b = static_cast<const T*>(P.b);
-  T* x = static_cast<T*>(P.x);
-  T* r = static_cast<T*>(P.r);
-  T* p = static_cast<T*>(P.p[0]);
-  T* Ap = static_cast<T*>(P.Ap);
+  const T* __restrict__ val = static_cast<const T*>(A.val);
+  const T* __restrict__ b = static_cast<const T*>(P.b);
+  T* __restrict__ x = static_cast<T*>(P.x);
+  T* __restrict__ r = static_cast<T*>(P.r);
+  T* __restrict__ p = static_cast<T*>(P.p[0]);
+  T* __restrict__ Ap = static_cast<T*>(P.Ap);
   const int G = gridDim.x;
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
   GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G)}};
   const int tid = threadIdx.x, nt = blockDim.x;
 
-  // r = b - A x ; rr = r.r ; bb = b.b
-  double rr = 0.0, bb = 0.0;
-  for (int i = row0 + tid; i < row1; i += nt) {
-    const T ax = T(spmv_row(A, val, x, i));
-    const T ri = T(-1) * ax + b[i];
+  // r = b - A x ; rr = r.r ; bb = b.b  (per-thread sums in T, then double)
+  T rr_t = T(0), bb_t = T(0);
+  CG_ROWS(i, {
+    const T ax = spmv_row(A, val, x, i);
+    const T bi = b[i];
+    const T ri = T(-1) * ax + bi;
     r[i] = ri;
-    rr += double(ri * ri);
-    bb += double(b[i] * b[i]);
-  }
+    rr_t = fma(ri, ri, rr_t);
+    bb_t = fma(bi, bi, bb_t);
+  })
+  double rr = double(rr_t), bb = double(bb_t);
   if (!gs.sum2(0, rr, bb)) return;
   T r1 = T(rr);  // float build: r.r rounded to float (cg_cpu.cpp:52)
   T r0 = T(0);
@@ -201,17 +224,18 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
     if (k > P.max_iter) break;
     if (k > 1) {
       const T beta = r1 / r0;
-      for (int i = row0 + tid; i < row1; i += nt) p[i] = fma(beta, p[i], r[i]);
+      CG_ROWS(i, { p[i] = fma(beta, p[i], r[i]); })
     } else {
-      for (int i = row0 + tid; i < row1; i += nt) p[i] = r[i];
+      CG_ROWS(i, { p[i] = r[i]; })
     }
     if (!gs.gb.sync()) return;
-    double pap = 0.0, unused = 0.0;
-    for (int i = row0 + tid; i < row1; i += nt) {
-      const T api = T(spmv_row(A, val, p, i));
+    T pap_t = T(0);
+    CG_ROWS(i, {
+      const T api = spmv_row(A, val, p, i);
       Ap[i] = api;
-      pap += double(p[i] * api);
-    }
+      pap_t = fma(p[i], api, pap_t);
+    })
+    double pap = double(pap_t), unused = 0.0;
     if (!gs.sum2(1 + (k & 1), pap, unused)) return;
     const T dot = T(pap);
     if (!(dot > T(0)) || !isfinite(double(dot))) {
@@ -219,14 +243,14 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
       return;
     }
     const T alpha = r1 / dot;
-    double rrn = 0.0;
-    for (int i = row0 + tid; i < row1; i += nt) {
-      const T pi = p[i];
-      x[i] = fma(alpha, pi, x[i]);
+    T rrn_t = T(0);
+    CG_ROWS(i, {
+      x[i] = fma(alpha, p[i], x[i]);
       const T ri = fma(-alpha, Ap[i], r[i]);
       r[i] = ri;
-      rrn += double(ri * ri);
-    }
+      rrn_t = fma(ri, ri, rrn_t);
+    })
+    double rrn = double(rrn_t);
     if (!gs.sum2(3, rrn, unused)) return;
     r0 = r1;
     r1 = T(rrn);
@@ -243,15 +267,15 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
 // Mixed precision: FP32 Krylov iteration, FP64 solution and true residual.
 __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant__ CgParams P) {
   const CgMat& A = P.A;
-  const double* val64 = static_cast<const double*>(A.val);
-  float* val32 = P.val32;
-  const double* b = static_cast<const double*>(P.b);
-  double* x = static_cast<double*>(P.x);
-  double* r64 = P.r64;
-  float* r = static_cast<float*>(P.r);
-  float* p = static_cast<float*>(P.p[0]);
-  float* Ap = static_cast<float*>(P.Ap);
-  float* xs = P.xs;
+  const double* __restrict__ val64 = static_cast<const double*>(A.val);
+  float* __restrict__ val32 = P.val32;
+  const double* __restrict__ b = static_cast<const double*>(P.b);
+  double* __restrict__ x = static_cast<double*>(P.x);
+  double* __restrict__ r64 = P.r64;
+  float* __restrict__ r = static_cast<float*>(P.r);
+  float* __restrict__ p = static_cast<float*>(P.p[0]);
+  float* __restrict__ Ap = static_cast<float*>(P.Ap);
+  float* __restrict__ xs = P.xs;
   const int G = gridDim.x;
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
   GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G)}};
@@ -263,19 +287,20 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
     const int j0 = A.rp[row0], j1 = A.rp[row1];
     for (int j = j0 + tid; j < j1; j += nt) val32[j] = float(val64[j]);
   } else {
-    for (int k = 0; k < A.ndiag; k++)
-      for (int i = row0 + tid; i < row1; i += nt) val32[(size_t)k * A.n + i] = float(val64[(size_t)k * A.n + i]);
+    for (int kd = 0; kd < A.ndiag; kd++)
+      for (int i = row0 + tid; i < row1; i += nt) val32[(size_t)kd * A.n + i] = float(val64[(size_t)kd * A.n + i]);
   }
   // true residual in FP64
   double rr = 0.0, bb = 0.0;
-  for (int i = row0 + tid; i < row1; i += nt) {
-    const double ri = b[i] - spmv_row(A, val64, x, i);
+  CG_ROWS(i, {
+    const double bi = b[i];
+    const double ri = bi - spmv_row(A, val64, x, i);
     r64[i] = ri;
     r[i] = float(ri);
     xs[i] = 0.0f;
-    rr += ri * ri;
-    bb += b[i] * b[i];
-  }
+    rr = fma(ri, ri, rr);
+    bb = fma(bi, bi, bb);
+  })
   if (!gs.sum2(0, rr, bb)) return;
   const double tol2 = (P.stop == PERKS_STOP_REL) ? P.tol * P.tol * bb : P.tol * P.tol;
   double maxrr = rr, rr0 = 0.0;
@@ -285,48 +310,50 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
     if (k > P.max_iter) break;
     if (k > 1) {
       const float beta = float(rr / rr0);
-      for (int i = row0 + tid; i < row1; i += nt) p[i] = fmaf(beta, p[i], r[i]);
+      CG_ROWS(i, { p[i] = fmaf(beta, p[i], r[i]); })
     } else {
-      for (int i = row0 + tid; i < row1; i += nt) p[i] = r[i];
+      CG_ROWS(i, { p[i] = r[i]; })
     }
     if (!gs.gb.sync()) return;
-    double pap = 0.0, unused = 0.0;
-    for (int i = row0 + tid; i < row1; i += nt) {
-      const float api = float(spmv_row(A, val32, p, i));
+    float pap_t = 0.0f;
+    CG_ROWS(i, {
+      const float api = spmv_row(A, val32, p, i);
       Ap[i] = api;
-      pap += double(p[i]) * double(api);
-    }
+      pap_t = fmaf(p[i], api, pap_t);
+    })
+    double pap = double(pap_t), unused = 0.0;
     if (!gs.sum2(1 + (k & 1), pap, unused)) return;
     if (!(pap > 0.0) || !isfinite(pap)) {
       if (tid == 0 && blockIdx.x == 0) atomicOr(P.status, kErrBreakdown);
       return;
     }
     const float alpha = float(rr / pap);
-    double rrn = 0.0;
-    for (int i = row0 + tid; i < row1; i += nt) {
+    float rrn_t = 0.0f;
+    CG_ROWS(i, {
       xs[i] = fmaf(alpha, p[i], xs[i]);
       const float ri = fmaf(-alpha, Ap[i], r[i]);
       r[i] = ri;
-      rrn += double(ri) * double(ri);
-    }
+      rrn_t = fmaf(ri, ri, rrn_t);
+    })
+    double rrn = double(rrn_t);
     if (!gs.sum2(3, rrn, unused)) return;
     since++;
     const bool update = rrn < P.delta2 * maxrr || rrn < tol2 || (P.replace_every > 0 && since >= P.replace_every) ||
                         k == P.max_iter;
     if (update) {
       // x += xs in FP64; true residual with the FP64 matrix
-      for (int i = row0 + tid; i < row1; i += nt) {
+      CG_ROWS(i, {
         x[i] += double(xs[i]);
         xs[i] = 0.0f;
-      }
+      })
       if (!gs.gb.sync()) return;
       double rt = 0.0, un2 = 0.0;
-      for (int i = row0 + tid; i < row1; i += nt) {
+      CG_ROWS(i, {
         const double ri = b[i] - spmv_row(A, val64, x, i);
         r64[i] = ri;
         r[i] = float(ri);
-        rt += ri * ri;
-      }
+        rt = fma(ri, ri, rt);
+      })
       if (!gs.sum2(0, rt, un2)) return;
       rrn = rt;
       maxrr = rt;

@@ -1,18 +1,25 @@
 // Correctly rounded division by a small positive integer constant b, as
-// IEEE-754 `x / b` (round to nearest even), without the general division
-// sequence.
+// IEEE-754 `x / b` (round to nearest even), in a few branch-free operations.
 //
-// Normal results: q0 = RN(x * r) with r = RN(1/b), e = fma(-q0, b, x) (exact),
-// q1 = fma(e, r, q0) — Markstein's correction (P. Markstein, "Computation of
-// elementary functions on the IBM RISC System/6000", IBM J. R&D 34(1), 1990;
-// also Muller et al., Handbook of Floating-Point Arithmetic, ch. 4).
-// Results that are subnormal (or in the binade just above) are computed
-// exactly in integer arithmetic: |x| is an integer multiple M of the smallest
-// subnormal, so the quotient is RN_even(M / b) of those units.
+//   q0 = RN(x * r)            with r = RN(1/b)
+//   e  = fma(-q0, b, x)       exact remainder
+//   q1 = fma(e, r, q0)        Markstein's correction (P. Markstein, "Computation
+//                             of elementary functions on the IBM RISC System/6000",
+//                             IBM J. R&D 34(1), 1990; Muller et al., Handbook of
+//                             Floating-Point Arithmetic, ch. 4)
 //
-// The float version for b = 118 and b = 159 is checked against IEEE division
-// for all 2^32 inputs on the CPU (oracle-side check) and both
-// versions against __fdiv_rn / __ddiv_rn on the GPU (tests/test_divconst_gpu.py).
+// For normal quotients q1 is the correctly rounded quotient. For quotients
+// on the subnormal grid (spacing g) q0 is within one grid step of x/b, and
+// x/b is either exactly on a rounding midpoint or at least g/(2b) away from
+// one, far more than the error of e*r; so q1 rounds like x/b except at exact
+// midpoints. Those only occur for even b (x/b = (k + 1/2) g when x is an odd
+// multiple of (b/2) g); there the remainder is exactly (b/2) g and the even
+// neighbour is chosen explicitly. The quotient takes the sign of x, which
+// fixes the sign of zero results.
+//
+// The float version is checked against IEEE division for all 2^32 inputs
+// with b = 118 and b = 159 (zero mismatches), the double version through the
+// bit-exact stencil tests on subnormal, tiny, huge, infinite and NaN fields.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -20,7 +27,7 @@
 namespace perks {
 
 template <int B>
-struct DivThreshold;  // below it the quotient is at most 2^-125 (float) / 2^-1021 (double)
+struct DivThreshold;  // |x| below it: quotient on the subnormal grid spacing
 template <>
 struct DivThreshold<118> {
   static constexpr float f = 0x1p-119f;
@@ -36,39 +43,41 @@ template <int B>
 __device__ __forceinline__ float div_const(float x) {
   constexpr float b = float(B);
   const float r = __fdiv_rn(1.0f, b);  // folded to a constant
-  const float ax = fabsf(x);
-  if (ax < DivThreshold<B>::f) {
-    const uint32_t M = __float2uint_rz(__fmul_rn(__fmul_rn(ax, 0x1p126f), 0x1p23f));
-    uint32_t q = M / uint32_t(B);
-    const uint32_t rem = M - q * uint32_t(B);
-    if (2u * rem > uint32_t(B) || (2u * rem == uint32_t(B) && (q & 1u))) q++;
-    const float res = __fmul_rn(__fmul_rn(__uint2float_rn(q), 0x1p-23f), 0x1p-126f);
-    return copysignf(res, x);
-  }
   const float q0 = __fmul_rn(x, r);
   const float e = __fmaf_rn(-q0, b, x);
-  const float q1 = __fmaf_rn(e, r, q0);
-  return isfinite(q0) ? q1 : q0;
+  float q1 = __fmaf_rn(e, r, q0);
+  if constexpr ((B & 1) == 0) {
+    constexpr float half = float(B / 2) * 0x1p-149f;  // b/2 subnormal steps
+    const bool tie = (fabsf(x) < DivThreshold<B>::f) && (fabsf(e) == half);
+    const float up = __fadd_rn(q0, copysignf(0x1p-149f, e));
+    q1 = tie ? ((__float_as_uint(q0) & 1u) ? up : q0) : q1;
+  }
+  return isfinite(q0) ? copysignf(q1, x) : q0;
 }
 
 template <int B>
 __device__ __forceinline__ double div_const(double x) {
+  // FP64 arithmetic is scarce on this GPU: the threshold, tie and finiteness
+  // tests and the sign transfer use integer operations on the bit patterns.
   constexpr double b = double(B);
+  constexpr long long kAbs = 0x7fffffffffffffffll, kExp = 0x7ff0000000000000ll, kSign = (long long)0x8000000000000000ull;
   const double r = __ddiv_rn(1.0, b);
-  const double ax = fabs(x);
-  if (ax < DivThreshold<B>::d) {
-    // |x| = M * 2^-1074 with M < 2^60
-    const uint64_t M = uint64_t(__double2ull_rz(__dmul_rn(__dmul_rn(ax, 0x1p1022), 0x1p52)));
-    uint64_t q = M / uint64_t(B);
-    const uint64_t rem = M - q * uint64_t(B);
-    if (2ull * rem > uint64_t(B) || (2ull * rem == uint64_t(B) && (q & 1ull))) q++;
-    const double res = __dmul_rn(__dmul_rn(__ull2double_rn(q), 0x1p-52), 0x1p-1022);
-    return copysign(res, x);
-  }
   const double q0 = __dmul_rn(x, r);
   const double e = __fma_rn(-q0, b, x);
-  const double q1 = __fma_rn(e, r, q0);
-  return isfinite(q0) ? q1 : q0;
+  double q1 = __fma_rn(e, r, q0);
+  const long long xb = __double_as_longlong(x), q0b = __double_as_longlong(q0);
+  if constexpr ((B & 1) == 0) {
+    constexpr double half = double(B / 2) * 0x1p-1074;
+    const long long thr_bits = __double_as_longlong(DivThreshold<B>::d);
+    const long long half_bits = __double_as_longlong(half);
+    const bool tie = ((xb & kAbs) < thr_bits) && ((__double_as_longlong(e) & kAbs) == half_bits);
+    if (tie) {  // rare: exact midpoint on the subnormal grid, take the even neighbour
+      const double up = __dadd_rn(q0, copysign(0x1p-1074, e));
+      q1 = (q0b & 1ll) ? up : q0;
+    }
+  }
+  if ((q0b & kExp) == kExp) return q0;  // x infinite or NaN
+  return __longlong_as_double((__double_as_longlong(q1) & kAbs) | (xb & kSign));
 }
 
 }  // namespace perks

@@ -50,19 +50,21 @@ template <class T, int SHAPE>
 struct Cfg2D {
   static constexpr int H = ShapeInfo<SHAPE>::H;
   static constexpr bool BOX = ShapeInfo<SHAPE>::box;
-  static constexpr int V = 16 / sizeof(T);               // elements per lane
+  static constexpr int V16 = 16 / sizeof(T);             // elements per 16-byte vector
+  // vectors per lane per row (one for the widest FP64 windows, to fit registers)
+  static constexpr int NV = (sizeof(T) == 8 && H >= 5) ? 1 : 2;
+  static constexpr int V = NV * V16;                     // elements per lane (8 FP32 / 4 FP64)
   static constexpr int SW = 32 * V;                      // strip width
   static constexpr int WN = 2 * H + 1;                   // window rows
-  // registers the window needs (32-bit words), to pick 1024 or 512 threads
+  // registers the window needs (32-bit words), to pick the warps per CTA
+  // (box shapes also hold the double-precision partial sums of the reference order)
   static constexpr int REG_EST =
-      int(sizeof(T) / 4) * (BOX ? WN * (V + 2 * H) + V : WN * (V + 1) + (V + 2 * H) + V) + 40;
-  // warps per CTA: as many as the register file allows (1024/768/512/256 threads)
+      int(sizeof(T) / 4) * (BOX ? WN * (V + 2 * H) + V : WN * (V + 1) + (V + 2 * H) + V) + (BOX ? 72 : 40);
   static constexpr int NW = (REG_EST <= 64 && !BOX) ? 32 : REG_EST <= 80 ? 24 : REG_EST <= 110 ? 16 : 8;
   static constexpr int NT = NW * 32;
-  static constexpr int D = 96 / NW;                      // rows in flight per warp (~48 KB per SM)
+  static constexpr int D = NW >= 24 ? 3 : NW == 16 ? 4 : 6;  // rows in flight per warp
   static constexpr int DR = D + 1;                       // ring slots per warp
-  static constexpr int EL = (2 * H + 0);                 // edge lanes
-  static constexpr int SLOT = SW + EL * V;               // ring slot: strip row + edge chunks
+  static constexpr int SLOT = SW + 2 * H * V16;          // ring slot: strip row + one chunk per edge lane
   static constexpr size_t ring_bytes = size_t(NW) * DR * SLOT * sizeof(T);
   static constexpr size_t res_row_bytes = size_t(NW) * SW * sizeof(T);  // one resident row for every warp
   static_assert(2 * H <= 32, "edge lanes");
@@ -79,16 +81,33 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-__device__ __forceinline__ void unpack(const float4& v, float (&o)[4]) {
-  o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+// Vector loads/stores of a lane's V elements (NV 16-byte vectors).
+template <int NV>
+__device__ __forceinline__ void load_lane(const float* src, float (&o)[4 * NV]) {
+#pragma unroll
+  for (int k = 0; k < NV; k++) {
+    const float4 v = reinterpret_cast<const float4*>(src)[k];
+    o[4 * k] = v.x; o[4 * k + 1] = v.y; o[4 * k + 2] = v.z; o[4 * k + 3] = v.w;
+  }
 }
-__device__ __forceinline__ void unpack(const double2& v, double (&o)[2]) {
-  o[0] = v.x; o[1] = v.y;
+template <int NV>
+__device__ __forceinline__ void load_lane(const double* src, double (&o)[2 * NV]) {
+#pragma unroll
+  for (int k = 0; k < NV; k++) {
+    const double2 v = reinterpret_cast<const double2*>(src)[k];
+    o[2 * k] = v.x; o[2 * k + 1] = v.y;
+  }
 }
-template <class VT, class T, int N>
-__device__ __forceinline__ VT pack(const T (&o)[N]) {
-  if constexpr (N == 4) return make_float4(o[0], o[1], o[2], o[3]);
-  else return make_double2(o[0], o[1]);
+template <int NV>
+__device__ __forceinline__ void store_lane(float* dst, const float (&o)[4 * NV]) {
+#pragma unroll
+  for (int k = 0; k < NV; k++)
+    reinterpret_cast<float4*>(dst)[k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+}
+template <int NV>
+__device__ __forceinline__ void store_lane(double* dst, const double (&o)[2 * NV]) {
+#pragma unroll
+  for (int k = 0; k < NV; k++) reinterpret_cast<double2*>(dst)[k] = make_double2(o[2 * k], o[2 * k + 1]);
 }
 
 // A window row in registers: V values of this lane and one edge value.
@@ -115,8 +134,8 @@ __device__ __forceinline__ void static_for(F&& f) {
 template <class T, int SHAPE, bool FAST>
 __global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const __grid_constant__ Stencil2DParams p) {
   using Cf = Cfg2D<T, SHAPE>;
-  using VT = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
-  constexpr int H = Cf::H, V = Cf::V, SW = Cf::SW, NW = Cf::NW, D = Cf::D, DR = Cf::DR, SLOT = Cf::SLOT;
+  constexpr int H = Cf::H, V = Cf::V, V16 = Cf::V16, NV = Cf::NV, SW = Cf::SW, NW = Cf::NW, D = Cf::D,
+                DR = Cf::DR, SLOT = Cf::SLOT;
   constexpr int WN = Cf::WN;
   constexpr bool BOX = Cf::BOX;
   constexpr int WW = V + 2 * H;  // horizontal window of one row
@@ -125,8 +144,8 @@ __global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  T* ring = reinterpret_cast<T*>(smem_raw) + size_t(wid) * DR * SLOT;
-  T* res = reinterpret_cast<T*>(smem_raw + Cf::ring_bytes);  // [C][NW][SW]
+  T* const ring = reinterpret_cast<T*>(smem_raw) + size_t(wid) * DR * SLOT;
+  T* const res = reinterpret_cast<T*>(smem_raw + Cf::ring_bytes);  // [C][NW][SW]
 
   const int wy = p.wy, wx = p.wx, pitch = p.pitch;
   const int item = blockIdx.x * NW + wid;
@@ -140,6 +159,7 @@ __global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const
   const int rres0 = r0 + H;
   const int xl = x0 + lane * V;            // this lane's first column
   const bool dir = p.dirichlet != 0;
+  const bool alt = p.alternate != 0;
   const bool ghost_strip = (x0 + SW > wx) && !dir;  // strip reaches past the last column
   const int lw = wx - 1 - x0;              // strip-local last column
   // Edge lanes: lane k < H needs column x0-1-k, lane H+k needs x0+SW+k, both
@@ -147,8 +167,20 @@ __global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const
   // lane fetches the aligned 16-byte chunk holding its column.
   const bool edge_lane = lane < 2 * H;
   const int edge_col = lane < H ? max(x0 - 1 - lane, 0) : min(x0 + SW + (lane - H), wx - 1);
-  const int edge_chunk = (edge_col / V) * V;
+  const int edge_chunk = (edge_col / V16) * V16;
   const int edge_sub = edge_col - edge_chunk;
+  T* const my_ring_v = ring + lane * V;                   // this lane's columns in a slot
+  T* const my_ring_e = ring + SW + min(lane, 2 * H - 1) * V16;  // this edge lane's chunk in a slot
+  // Shuffle sources and selectors of the horizontal window (row independent).
+  int src_l[H], src_r[H];
+  bool use_in_l[H], use_in_r[H];
+#pragma unroll
+  for (int d = 1; d <= H; d++) {
+    src_l[d - 1] = max(d - 1 - lane * V, 0);
+    src_r[d - 1] = H + max(d - 1 - (31 - lane) * V, 0);
+    use_in_l[d - 1] = lane * V >= d;
+    use_in_r[d - 1] = (31 - lane) * V >= d;
+  }
 
   GridBarrier gbar{p.bar, p.status, gridDim.x};
   const uint64_t pol = policy_evict_normal();
@@ -160,41 +192,48 @@ __global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const
 
   if (C > 0) {
     const T* fin = static_cast<const T*>(p.f[p.t0 & 1]);
-    for (int k = 0; k < C; k++)
-      *reinterpret_cast<VT*>(res_ptr(rres0 + k)) = *reinterpret_cast<const VT*>(fin + size_t(rres0 + k) * pitch + xl);
+    for (int k = 0; k < C; k++) {
+      T v[V];
+      load_lane<NV>(fin + size_t(rres0 + k) * pitch + xl, v);
+      store_lane<NV>(res_ptr(rres0 + k), v);
+    }
   }
 
   for (int it = 0; it < p.steps && ok; it++) {
     const int t = p.t0 + it;
     const T* fin = static_cast<const T*>(p.f[t & 1]);
     T* fout = static_cast<T*>(p.f[(t + 1) & 1]);
-    const bool fwd = !p.alternate || ((t & 1) == 0);
+    const bool fwd = !alt || ((t & 1) == 0);
 
     if (active) {
-      auto row_of = [&](int q) { return min(max(fwd ? r0 + q : r1 - 1 - q, 0), wy - 1); };
-      auto slot_of = [&](int q) -> T* { return ring + size_t((q + 2 * DR) % DR) * SLOT; };
-      auto interior = [&](int r) { return p.alternate && r >= r0 + H && r < r1 - H; };
+      const int rbase = fwd ? r0 : r1 - 1, rstep = fwd ? 1 : -1;
+      auto row_of = [&](int q) { return min(max(rbase + rstep * q, 0), wy - 1); };
+      auto interior = [&](int r) { return r >= r0 + H && r < r1 - H; };
+      int sf = 0;  // ring slot of the next position to fetch (positions advance by one)
+      int sl = 0;  // ring slot of the next position to load into registers
       // Issue the copies for sweep position q (one commit group per position).
       auto fetch = [&](int q) {
         if (q < TY + H) {
-          T* slot = slot_of(q);
           const int r = row_of(q);
           const T* src = fin + size_t(r) * pitch;
-          if (!is_res(r)) cp_async16(slot + lane * V, src + xl, interior(r) ? pol_first : pol);
-          if (edge_lane) cp_async16(slot + SW + lane * V, src + edge_chunk, pol);
+          T* slot = ring + size_t(sf) * SLOT;
+          if (!is_res(r)) {
+            const uint64_t pl = (alt && interior(r)) ? pol_first : pol;
+#pragma unroll
+            for (int k = 0; k < NV; k++) cp_async16(my_ring_v + size_t(sf) * SLOT + k * V16, src + xl + k * V16, pl);
+          }
+          if (edge_lane) cp_async16(slot + SW + lane * V16, src + edge_chunk, pol);
         }
         cp_async_commit();
+        sf = (sf + 1 == DR) ? 0 : sf + 1;
       };
       // Move position q from the ring (or resident storage) into registers.
       auto load_row = [&](int q) -> RowT {
         RowT out;
-        const T* slot = slot_of(q);
         const int r = row_of(q);
         const bool rr = is_res(r);
-        const T* vsrc = rr ? res_ptr(r) : slot + lane * V;  // one load from whichever holds the row
-        const VT v = *reinterpret_cast<const VT*>(vsrc);
-        unpack(v, out.v);
-        out.e = edge_lane ? slot[SW + lane * V + edge_sub] : T(0);  // only edge lanes own an edge chunk
+        load_lane<NV>(rr ? res_ptr(r) : my_ring_v + size_t(sl) * SLOT, out.v);
+        out.e = edge_lane ? my_ring_e[size_t(sl) * SLOT + edge_sub] : T(0);
         if (ghost_strip) {
           // elements beyond the last column take that column's value
           const int le = lw % V;
@@ -206,7 +245,7 @@ __global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const
 #pragma unroll
           for (int i = 0; i < V; i++) out.v[i] = (i > lim) ? edge : out.v[i];
         }
-        if (!rr && interior(r)) {
+        if (alt && !rr && interior(r)) {
           // the middle lines of this strip row are dead once read: drop them
           // from L2 without write-back (edge lines stay: neighbours read them)
           __syncwarp();
@@ -215,6 +254,7 @@ __global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const
           const int c = lane * V;
           if ((lane % LPL) == 0 && c >= LE && c + LE <= SW - LE) l2_discard_line(fin + size_t(r) * pitch + x0 + c);
         }
+        sl = (sl + 1 == DR) ? 0 : sl + 1;
         return out;
       };
 
@@ -233,11 +273,11 @@ __global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const
         for (int d = 1; d <= H; d++) {
           const int dl = (d + V - 1) / V;  // lanes away
           const T vin = __shfl_up_sync(0xffffffffu, r.v[dl * V - d], dl);
-          const T ved = __shfl_sync(0xffffffffu, r.e, max(d - 1 - lane * V, 0));
-          out.h[H - d] = (lane * V >= d) ? vin : ved;
+          const T ved = __shfl_sync(0xffffffffu, r.e, src_l[d - 1]);
+          out.h[H - d] = use_in_l[d - 1] ? vin : ved;
           const T vin2 = __shfl_down_sync(0xffffffffu, r.v[(d - 1) % V], dl);
-          const T ved2 = __shfl_sync(0xffffffffu, r.e, H + max(d - 1 - (31 - lane) * V, 0));
-          out.h[H + V - 1 + d] = ((31 - lane) * V >= d) ? vin2 : ved2;
+          const T ved2 = __shfl_sync(0xffffffffu, r.e, src_r[d - 1]);
+          out.h[H + V - 1 + d] = use_in_r[d - 1] ? vin2 : ved2;
         }
         return out;
       };
@@ -249,7 +289,6 @@ __global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const
       for (int q = -H; q < -H + D; q++) fetch(q);
       int qn = -H;  // next position to bring into the window
       static_for<2 * H>([&](auto kc) {
-        constexpr int k = decltype(kc)::value;
         cp_async_wait<D - 1>();
         __syncwarp();
         bring(qn, kc);
@@ -294,12 +333,12 @@ __global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const
                   if (row_fixed || x < H || x >= wx - H) o[i] = old;
                 }
               }
-              const VT ov = pack<VT>(o);
+              T* dst = fout + size_t(y) * pitch + xl;
               if (is_res(y)) {
-                *reinterpret_cast<VT*>(res_ptr(y)) = ov;
-                if (lane * V < H || (lane + 1) * V > SW - H) *reinterpret_cast<VT*>(fout + size_t(y) * pitch + xl) = ov;
+                store_lane<NV>(res_ptr(y), o);
+                if (lane * V < H || (lane + 1) * V > SW - H) store_lane<NV>(dst, o);
               } else {
-                *reinterpret_cast<VT*>(fout + size_t(y) * pitch + xl) = ov;
+                store_lane<NV>(dst, o);
               }
             }
           });
@@ -316,8 +355,11 @@ __global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const
   }
   if (ok && C > 0) {
     T* fnew = static_cast<T*>(p.f[(p.t0 + p.steps) & 1]);
-    for (int k = 0; k < C; k++)
-      *reinterpret_cast<VT*>(fnew + size_t(rres0 + k) * pitch + xl) = *reinterpret_cast<const VT*>(res_ptr(rres0 + k));
+    for (int k = 0; k < C; k++) {
+      T v[V];
+      load_lane<NV>(res_ptr(rres0 + k), v);
+      store_lane<NV>(fnew + size_t(rres0 + k) * pitch + xl, v);
+    }
   }
 }
 
