@@ -14,8 +14,10 @@
 // one, far more than the error of e*r; so q1 rounds like x/b except at exact
 // midpoints. Those only occur for even b (x/b = (k + 1/2) g when x is an odd
 // multiple of (b/2) g); there the remainder is exactly (b/2) g and the even
-// neighbour is chosen explicitly. The quotient takes the sign of x, which
-// fixes the sign of zero results.
+// neighbour is chosen explicitly. A remainder of exactly (b/2) g is only
+// possible while ulp(q0) = g (for larger quotients the remainder is a multiple
+// of 2g and b/2 is odd), so the test needs no magnitude check. The quotient
+// takes the sign of x, which fixes the sign of zero results.
 //
 // The float version is checked against IEEE division for all 2^32 inputs
 // with b = 118 and b = 159 (zero mismatches), the double version through the
@@ -27,19 +29,6 @@
 namespace perks {
 
 template <int B>
-struct DivThreshold;  // |x| below it: quotient on the subnormal grid spacing
-template <>
-struct DivThreshold<118> {
-  static constexpr float f = 0x1p-119f;
-  static constexpr double d = 0x1p-1015;
-};
-template <>
-struct DivThreshold<159> {
-  static constexpr float f = 0x1p-118f;
-  static constexpr double d = 0x1p-1014;
-};
-
-template <int B>
 __device__ __forceinline__ float div_const(float x) {
   constexpr float b = float(B);
   const float r = __fdiv_rn(1.0f, b);  // folded to a constant
@@ -48,7 +37,7 @@ __device__ __forceinline__ float div_const(float x) {
   float q1 = __fmaf_rn(e, r, q0);
   if constexpr ((B & 1) == 0) {
     constexpr float half = float(B / 2) * 0x1p-149f;  // b/2 subnormal steps
-    const bool tie = (fabsf(x) < DivThreshold<B>::f) && (fabsf(e) == half);
+    const bool tie = fabsf(e) == half;
     const float up = __fadd_rn(q0, copysignf(0x1p-149f, e));
     q1 = tie ? ((__float_as_uint(q0) & 1u) ? up : q0) : q1;
   }
@@ -57,7 +46,7 @@ __device__ __forceinline__ float div_const(float x) {
 
 template <int B>
 __device__ __forceinline__ double div_const(double x) {
-  // FP64 arithmetic is scarce on this GPU: the threshold, tie and finiteness
+  // FP64 arithmetic is scarce on this GPU: the tie and finiteness
   // tests and the sign transfer use integer operations on the bit patterns.
   constexpr double b = double(B);
   constexpr long long kAbs = 0x7fffffffffffffffll, kExp = 0x7ff0000000000000ll, kSign = (long long)0x8000000000000000ull;
@@ -68,9 +57,8 @@ __device__ __forceinline__ double div_const(double x) {
   const long long xb = __double_as_longlong(x), q0b = __double_as_longlong(q0);
   if constexpr ((B & 1) == 0) {
     constexpr double half = double(B / 2) * 0x1p-1074;
-    const long long thr_bits = __double_as_longlong(DivThreshold<B>::d);
     const long long half_bits = __double_as_longlong(half);
-    const bool tie = ((xb & kAbs) < thr_bits) && ((__double_as_longlong(e) & kAbs) == half_bits);
+    const bool tie = (__double_as_longlong(e) & kAbs) == half_bits;
     if (tie) {  // rare: exact midpoint on the subnormal grid, take the even neighbour
       const double up = __dadd_rn(q0, copysign(0x1p-1074, e));
       q1 = (q0b & 1ll) ? up : q0;
