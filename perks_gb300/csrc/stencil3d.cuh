@@ -1,39 +1,62 @@
-// 3D Jacobi time loop for sm_103a: z-streaming persistent cooperative kernel
-// with a TMA (cp.async.bulk.tensor) plane pipeline.
+// 3D Jacobi time loop for sm_103a: persistent cooperative kernel with a
+// warp-specialised plane pipeline.
 //
 // Work decomposition:
-//   The internal field is [height][width_y][pitch_x] (pitch_x = width_x
-//   rounded up to 16 bytes). CTA (tz, ty, tx) owns an x-y tile of TX x TY
-//   cells and a z-slab [z0, z1). Each step it sweeps the slab plane by plane
-//   in groups of R output planes. Input planes (tile plus H halo rows and HP
-//   halo columns on each side) arrive in a ring of NR shared-memory slots, one
-//   3D tiled TMA copy per plane; coordinates outside the field are zero-filled
-//   by the TMA unit and then overwritten with clamped values in shared memory.
-//   Each thread owns V consecutive columns of RY consecutive rows and keeps a
-//   rolling register window of 2H+1 planes.
-//   PERKS caching: planes [z0+H, z0+H+C) of the slab stay in shared memory for
-//   the whole launch with the same skewed in-place update as the 2D kernel;
-//   their tile-boundary rows and columns are stored to the field each step so
-//   that neighbouring tiles can load them, and their halo ring is reloaded
-//   from the field with four small TMA copies per plane per step.
-//   Steps are separated by a bounded grid barrier.
+//   The internal field is [height][width_y][px] (px = width_x rounded up to
+//   16 bytes). An x-y tile is SW columns (32 lanes x V elements) by TY rows.
+//   The (tile, plane) pairs of the whole domain, tile-major, are split into
+//   gridDim.x equal ranges; CTA b sweeps its range every step as one or two
+//   z-runs ("segments") of one tile each, so every SM gets the same number of
+//   cells whatever the domain's shape.
+//   A CTA has NWC compute warps and one producer warp. The producer copies
+//   each input plane of a segment (TY + 2H rows of SW + 2HP columns, one
+//   cp.async.bulk per row, spread over its lanes, clipped to the field) into a
+//   ring of NR shared-memory slots and completes the slot's "full" mbarrier.
+//   Compute warp w owns RY rows of the tile: for output plane z it reads
+//   planes z-H..z+H from the ring, keeps a rolling window of rows in
+//   registers, moves horizontal neighbours between lanes by shuffles, writes
+//   its rows of the output plane to the field, and arrives on the "empty"
+//   mbarrier (count NWC) of plane z-H, after which the producer may refill that
+//   slot. Nothing synchronises the whole CTA inside a step; steps are
+//   separated by one bounded grid barrier.
+//   With `alternate`, odd steps sweep the segments and their planes in reverse,
+//   so that the planes written last are read first while still in L2.
+//
+// Boundary: clamp-to-edge as the reference (plane, row and column indices
+// clamped), or Dirichlet (outer H cells keep their input value). Rows and
+// planes outside the domain are never copied.
 #pragma once
-#include <cuda.h>
 #include <cstdint>
+#include <type_traits>
 #include "ptx.cuh"
 #include "shapes.cuh"
+#include "stencil2d.cuh"  // static_for
 
 namespace perks {
 
+template <class T>
+__device__ __forceinline__ void vec16_load(const T* src, T* dst) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 v = *reinterpret_cast<const float4*>(src);
+    dst[0] = v.x; dst[1] = v.y; dst[2] = v.z; dst[3] = v.w;
+  } else {
+    const double2 v = *reinterpret_cast<const double2*>(src);
+    dst[0] = v.x; dst[1] = v.y;
+  }
+}
+template <class T>
+__device__ __forceinline__ void vec16_store(T* dst, const T* src) {
+  if constexpr (sizeof(T) == 4)
+    *reinterpret_cast<float4*>(dst) = make_float4(src[0], src[1], src[2], src[3]);
+  else
+    *reinterpret_cast<double2*>(dst) = make_double2(src[0], src[1]);
+}
+
 struct Stencil3DParams {
-  CUtensorMap map[2];     // plane box {TX+2HP, TY+2H, 1} over field 0 / 1
-  CUtensorMap mapNS[2];   // box {TX+2HP, H, 1}: north/south halo strips of resident planes
-  CUtensorMap mapWE[2];   // box {HP, TY, 1}: west/east halo strips of resident planes
   void* f[2];
-  int h, wy, wx, px;      // domain and x pitch (elements)
-  int gx, gy, gz;         // tile grid
+  int h, wy, wx, px;  // domain and x pitch (elements)
+  int gx, gy;         // x-y tile grid
   int steps, t0;
-  int C, M;               // resident planes per slab (upper bound) and slots
   int dirichlet, alternate, persistent;
   unsigned* bar;
   unsigned* status;
@@ -43,424 +66,313 @@ template <class T, int SHAPE>
 struct Cfg3D {
   static constexpr int H = ShapeInfo<SHAPE>::H;
   static constexpr bool BOX = ShapeInfo<SHAPE>::box;
-  static constexpr int V = 16 / sizeof(T);
-  static constexpr int NTX = (sizeof(T) == 4) ? 16 : 32;  // threads across x
-  static constexpr int NTY = 256 / NTX;                   // threads across y
-  static constexpr int NT = NTX * NTY;
-  static constexpr int RY = 2;                            // rows per thread
-  static constexpr int TX = NTX * V;                      // 64
-  static constexpr int TY = NTY * RY;                     // 32 (f32) / 16 (f64)
-  static constexpr int HP = ((H + V - 1) / V) * V;
-  static constexpr int RWX = TX + 2 * HP;                 // slot row width
+  static constexpr int V16 = 16 / sizeof(T);
+  static constexpr int NV = (BOX || H >= 2) ? 1 : 2;      // 16-byte vectors per lane
+  static constexpr int V = NV * V16;                      // columns per lane
+  static constexpr int SW = 32 * V;                       // tile width
+  static constexpr int HP = ((H + V16 - 1) / V16) * V16;  // pad columns each side (16-byte multiple)
+  // 8 compute warps + the producer: 9 warps leave 168 registers per thread
+  // (3 warps on the fullest SM sub-partition), enough for every window here
+  static constexpr int NWC = 8;
+  static constexpr int RY = 4;                            // rows per compute warp
+  static constexpr int TY = NWC * RY;                     // tile height
+  static constexpr int NT = (NWC + 1) * 32;
+  static constexpr int RWX = SW + 2 * HP;                 // slot row width
   static constexpr int SR = TY + 2 * H;                   // slot rows
-  static constexpr int PLANE = SR * RWX;                  // elements per plane tile
-  static constexpr int AL = 128 / sizeof(T);              // TMA destinations are 128-byte aligned
-  static constexpr int SLOT = ((PLANE + AL - 1) / AL) * AL;  // slot stride (elements)
-  static constexpr int SNS = ((H * RWX + AL - 1) / AL) * AL; // side-buffer strip strides
-  static constexpr int SWE = ((HP * TY + AL - 1) / AL) * AL;
-  static constexpr int SIDE = 2 * SNS + 2 * SWE;            // side buffer per resident plane
-  static constexpr int R = 4;                             // output planes per group
-  static constexpr int NR = 2 * R + 2 * H + 2;            // ring slots
-  static_assert(NR <= 64, "phase mask");
-  static constexpr size_t slot_bytes = size_t(SLOT) * sizeof(T);
-  static constexpr size_t box_bytes = size_t(PLANE) * sizeof(T);   // bytes one plane copy delivers
+  static constexpr int AL = 128 / sizeof(T);
+  static constexpr int PLANE = ((SR * RWX + AL - 1) / AL) * AL;  // slot stride (elements)
+  static constexpr size_t slot_bytes = size_t(PLANE) * sizeof(T);
+  // planes in flight beyond the 2H+1 being read: about 72 KB, at least 2,
+  // within a 200 KB ring
+  static constexpr int DMAX = int((200u * 1024u) / slot_bytes) - (2 * H + 1);
+  static constexpr int DWANT = int((72u * 1024u + slot_bytes - 1) / slot_bytes) > 2
+                                   ? int((72u * 1024u + slot_bytes - 1) / slot_bytes)
+                                   : 2;
+  static constexpr int D = DMAX < DWANT ? DMAX : DWANT;
+  static constexpr int NR = 2 * H + 1 + D;                // ring slots
   static constexpr size_t ring_bytes = size_t(NR) * slot_bytes;
-  static constexpr size_t bar_bytes = (NR + 2) * sizeof(uint64_t);
+  static constexpr size_t smem_bytes = ring_bytes + 2 * NR * sizeof(uint64_t);
+  static_assert(D >= 1, "ring too small");
+  static_assert(H <= V16, "horizontal neighbours are at most one lane away");
 };
-
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar,
-                                            uint64_t policy) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cta.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint"
-      " [%0], [%1, {%2, %3, %4}], [%5], %6;" ::"r"(smem_u32(dst)),
-      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar)), "l"(policy)
-      : "memory");
-}
 
 template <class T, int SHAPE, bool FAST>
 __global__ void __launch_bounds__(Cfg3D<T, SHAPE>::NT, 1)
     stencil3d_kernel(const __grid_constant__ Stencil3DParams p) {
   using Cf = Cfg3D<T, SHAPE>;
-  using VT = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
-  constexpr int H = Cf::H, V = Cf::V, TX = Cf::TX, TY = Cf::TY, HP = Cf::HP, RWX = Cf::RWX, SR = Cf::SR;
-  constexpr int PLANE = Cf::SLOT, R = Cf::R, NR = Cf::NR, RY = Cf::RY, NT = Cf::NT, NTX = Cf::NTX;
-  constexpr int NW = 2 * H + 1;     // planes in the rolling window
-  constexpr int WR = RY + 2 * H;    // window rows
-  constexpr int WC = V + 2 * H;     // window columns
+  constexpr int H = Cf::H, V = Cf::V, V16 = Cf::V16, NV = Cf::NV, SW = Cf::SW, HP = Cf::HP, RY = Cf::RY,
+                NWC = Cf::NWC, TY = Cf::TY, RWX = Cf::RWX, PLANE = Cf::PLANE, NR = Cf::NR;
+  constexpr bool BOX = Cf::BOX;
+  constexpr int WV = V16 + 2 * H;  // horizontal window of one vector
+  constexpr int NP = 2 * H + 1;    // planes one output reads
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  T* ring = reinterpret_cast<T*>(smem_raw);
-  T* res = ring + size_t(NR) * PLANE;
-  T* side = res + size_t(p.M) * PLANE;  // halo strips of resident planes, [C][N,S,W,E]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(side + size_t(p.M > 0 ? p.C : 0) * Cf::SIDE);
-  uint64_t* bar_res = bars + NR;
+  T* const ring = reinterpret_cast<T*>(smem_raw);
+  uint64_t* const full = reinterpret_cast<uint64_t*>(smem_raw + Cf::ring_bytes);
+  uint64_t* const empty = full + NR;
 
-  const int tid = threadIdx.x;
-  const int txi = tid % NTX, tyi = tid / NTX;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const bool producer = wid == NWC;
   const int h = p.h, wy = p.wy, wx = p.wx, px = p.px;
-  const int ntiles = p.gx * p.gy * p.gz;
-  // Geometry of the tile being swept (a CTA owns several tiles when the tile
-  // grid is larger than the launch; resident planes then stay off).
-  int x0 = 0, y0 = 0, z0 = 0, z1 = 0, ZN = 0, lw = 0, lwy = 0;
-  bool fix_l = false, fix_r = false, fix_t = false, fix_b = false, any_fix = false;
-  auto set_tile = [&](int b) {
-    const int tj = b % p.gx;
-    b /= p.gx;
-    const int ti = b % p.gy;
-    const int tk = b / p.gy;
-    x0 = tj * TX;
-    y0 = ti * TY;
-    z0 = int((long long)tk * h / p.gz);
-    z1 = int((long long)(tk + 1) * h / p.gz);
-    ZN = z1 - z0;
-    fix_l = !p.dirichlet && x0 == 0;
-    fix_r = !p.dirichlet && x0 + TX + HP > wx;
-    fix_t = !p.dirichlet && y0 == 0;
-    fix_b = !p.dirichlet && y0 + TY + H > wy;
-    any_fix = fix_l || fix_r || fix_t || fix_b;
-    lw = wx - 1 - x0;   // tile-local last column
-    lwy = wy - 1 - y0;  // tile-local last row
-  };
-  set_tile(blockIdx.x);
-  const int C = (p.M > 0 && ntiles == int(gridDim.x)) ? max(0, min(p.C, ZN - 2 * H)) : 0;
-  const int zres0 = z0 + H;
-  const int M = p.M;
-  const int cx = txi * V;      // thread's first column (tile-local)
-  const int cy = tyi * RY;     // thread's first row (tile-local)
+  const bool dir = p.dirichlet != 0;
+  const long long total = (long long)p.gx * p.gy * h;
+  const long long c_lo = total * blockIdx.x / gridDim.x, c_hi = total * (blockIdx.x + 1) / gridDim.x;
+  const int nseg = c_hi > c_lo ? int((c_hi - 1) / h - c_lo / h + 1) : 0;
 
-  GridBarrier gbar{p.bar, p.status, gridDim.x};
-  const uint64_t pol = policy_evict_normal();
-  const uint64_t pol_first = policy_evict_first();
-
-  if (tid == 0) {
-    for (int i = 0; i < NR + 1; i++) mbar_init(&bars[i], 1);
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < NR; i++) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], NWC);
+    }
     fence_mbar_init();
   }
   __syncthreads();
 
-  uint64_t phase = 0ull;
-  uint32_t res_phase = 0u;
-  int off = 0;
+  GridBarrier gbar{p.bar, p.status, gridDim.x};
+  const uint64_t pol = policy_evict_normal();
   bool ok = true;
-  int issued = 0, waited = 0;
-  bool fwd = true;
-
-  auto slot_of_res = [&](int z) -> T* {
-    int s = (z - zres0 + off) % M;
-    if (s < 0) s += M;
-    return res + size_t(s) * PLANE;
-  };
-  // Replace values outside the domain by clamped ones (columns first, then rows).
-  auto fixup_plane = [&](T* slot) {
-    if (fix_l || fix_r) {
-      for (int r = tid; r < SR; r += NT) {
-        T* row = slot + r * RWX;
-        if (fix_l) {
-          const T v = row[HP];
-          for (int k = 1; k <= H; k++) row[HP - k] = v;
-        }
-        if (fix_r && lw < TX + HP - 1) {
-          const T v = row[HP + lw];
-          for (int k = 1; k <= H && HP + lw + k < RWX; k++) row[HP + lw + k] = v;
-        }
-      }
-    }
-    if (fix_t || fix_b) {
-      __syncthreads();
-      for (int c = tid; c < RWX; c += NT) {
-        if (fix_t) {
-          const T v = slot[H * RWX + c];
-          for (int k = 1; k <= H; k++) slot[(H - k) * RWX + c] = v;
-        }
-        if (fix_b && lwy < TY + H - 1) {
-          const T v = slot[(H + lwy) * RWX + c];
-          for (int k = 1; k <= H && H + lwy + k < SR; k++) slot[(H + lwy + k) * RWX + c] = v;
-        }
-      }
-    }
-  };
-
-  int tmx = x0 - HP, tmy = y0 - H;  // TMA box origin
-
-  // ---------------------------------------------------------------- prologue
-  if (C > 0) {
-    const CUtensorMap* mp = &p.map[p.t0 & 1];
-    if (tid == 0) {
-      mbar_arrive_expect_tx(bar_res, unsigned(Cf::box_bytes) * unsigned(C));
-      for (int z = zres0; z < zres0 + C; z++) tma_load_3d(slot_of_res(z), mp, tmx, tmy, z, bar_res, pol);
-    }
-    if (!mbar_wait(bar_res, res_phase & 1u)) {
-      atomicOr(p.status, kErrCopyTimeout);
-      ok = false;
-    }
-    res_phase ^= 1u;
-    ok = __syncthreads_and(ok);
-    if (ok && any_fix) {
-      for (int k = 0; k < C; k++) fixup_plane(slot_of_res(zres0 + k));
-    }
-  }
+  // Positions: every plane a CTA loads gets the next global position P; its
+  // slot is P % NR, and the k-th use of a slot (k = P / NR) completes phase k
+  // of the slot's full barrier and, once all compute warps are done with it,
+  // phase k of its empty barrier.
+  long long pc = 0;      // positions of all finished segments
+  long long issued = 0;  // producer: positions issued so far
 
   for (int it = 0; it < p.steps && ok; it++) {
     const int t = p.t0 + it;
-    const CUtensorMap* mp = &p.map[t & 1];
+    const T* fin = static_cast<const T*>(p.f[t & 1]);
     T* fout = static_cast<T*>(p.f[(t + 1) & 1]);
-    fwd = !p.alternate || ((t & 1) == 0);
-    auto plane_of = [&](int s) { return fwd ? z0 + s : z1 - 1 - s; };
-    auto is_res = [&](int z) { return C > 0 && z >= zres0 && z < zres0 + C; };
-    auto loaded = [&](int s) {
-      const int z = plane_of(s);
-      return z >= 0 && z < h && !is_res(z);
-    };
-    auto pos_of = [&](int z) { return fwd ? z - z0 : z1 - 1 - z; };
-    auto slot_of = [&](int z) -> T* {
-      z = min(max(z, 0), h - 1);
-      if (is_res(z)) return slot_of_res(z);
-      return ring + size_t((pos_of(z) + H) % NR) * PLANE;
-    };
-    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-    if (tile != int(blockIdx.x)) {
-      set_tile(tile);
-      tmx = x0 - HP;
-      tmy = y0 - H;
-    }
-    __syncthreads();  // ring slots of the previous tile are no longer read
-    issued = -H;
-    auto produce = [&](int upto) {
-      const int lim = min(upto, ZN + H);
-      for (; issued < lim; issued++) {
-        if (!loaded(issued)) continue;
-        const int z = plane_of(issued);
-        const int q = (issued + H) % NR;
-        mbar_arrive_expect_tx(&bars[q], unsigned(Cf::box_bytes));
-        const bool interior = z >= z0 + H && z < z1 - H;
-        tma_load_3d(ring + size_t(q) * PLANE, mp, tmx, tmy, z, &bars[q], (p.alternate && interior) ? pol_first : pol);
-      }
-    };
-    if (tid == 0) {
-      fence_proxy_async_global();
-      produce(NR - H);
-      if (C > 0 && it > 0) {
-        // reload the halo ring of every resident plane into the side buffer
-        // (dense strips N, S, W, E); it is scattered into the slots below.
-        const unsigned bns = unsigned(H * RWX * sizeof(T)), bwe = unsigned(HP * TY * sizeof(T));
-        mbar_arrive_expect_tx(bar_res, (2 * bns + 2 * bwe) * unsigned(C));
-        for (int k = 0; k < C; k++) {
-          const int z = zres0 + k;
-          T* sd = side + size_t(k) * Cf::SIDE;
-          tma_load_3d(sd, &p.mapNS[t & 1], tmx, y0 - H, z, bar_res, pol);
-          tma_load_3d(sd + Cf::SNS, &p.mapNS[t & 1], tmx, y0 + TY, z, bar_res, pol);
-          tma_load_3d(sd + 2 * Cf::SNS, &p.mapWE[t & 1], x0 - HP, y0, z, bar_res, pol);
-          tma_load_3d(sd + 2 * Cf::SNS + Cf::SWE, &p.mapWE[t & 1], x0 + TX, y0, z, bar_res, pol);
-        }
-      }
-    }
-    if (C > 0 && it > 0) {
-      if (!mbar_wait(bar_res, res_phase & 1u)) {
-        atomicOr(p.status, kErrCopyTimeout);
-        ok = false;
-      }
-      res_phase ^= 1u;
-      ok = __syncthreads_and(ok);
-      if (!ok) break;
-      // N/S strips: H rows of RWX; W/E strips: TY rows of HP.
-      for (int i = tid; i < C * (2 * H * RWX + 2 * TY * HP); i += NT) {
-        const int per = 2 * H * RWX + 2 * TY * HP;
-        const int k = i / per;
-        int j = i % per;
-        T* sl = slot_of_res(zres0 + k);
-        const T* sd = side + size_t(k) * Cf::SIDE;
-        if (j < 2 * H * RWX) {
-          const int sdn = j / (H * RWX);  // 0 = north, 1 = south
-          const int e = j % (H * RWX);
-          sl[(sdn ? H + TY : 0) * RWX + e] = sd[sdn * Cf::SNS + e];
-        } else {
-          j -= 2 * H * RWX;
-          const int sde = j / (TY * HP);  // 0 = west, 1 = east
-          const int e = j % (TY * HP);
-          const int r = e / HP, c = e % HP;
-          sl[(H + r) * RWX + (sde ? HP + TX : 0) + c] = sd[2 * Cf::SNS + sde * Cf::SWE + e];
-        }
-      }
-      if (any_fix) {
-        __syncthreads();
-        for (int k = 0; k < C; k++) fixup_plane(slot_of_res(zres0 + k));
-      }
-    }
+    const bool fwd = !p.alternate || (t & 1) == 0;
+    if (producer && it > 0) fence_proxy_async_global();
+    for (int k = 0; k < nseg && ok; k++) {
+      const long long tb = c_lo / h + (fwd ? k : nseg - 1 - k);  // tile of this segment
+      const int z_lo = int(max(c_lo, tb * h) - tb * h), z_hi = int(min(c_hi, (tb + 1) * h) - tb * h);
+      const int ZN = z_hi - z_lo;
+      const int tile = int(tb);
+      const int x0 = (tile % p.gx) * SW, y0 = (tile / p.gx) * TY;
+      // segment position q in [-H, ZN+H) is global position pc + H + q
+      const int sb = int((pc + H) % NR);
+      const unsigned par0 = unsigned(((pc + H) / NR + 1) & 1);
+      auto slot_index = [&](int q) { return (sb + q + NR) % NR; };
+      auto slot_parity = [&](int q) { return (par0 + unsigned((sb + q + NR) / NR)) & 1u; };
 
-    waited = -H;
-    for (int lo = 0; lo < ZN && ok; lo += R) {
-      const int hi = min(lo + R, ZN);
-      const int need_hi = hi + H;
-      const int first_new = waited;
-      for (; waited < need_hi; waited++) {
-        if (!loaded(waited)) continue;
-        const int q = (waited + H) % NR;
-        if (!mbar_wait(&bars[q], unsigned(phase >> q) & 1u)) {
-          atomicOr(p.status, kErrCopyTimeout);
-          ok = false;
-          break;
-        }
-        phase ^= (1ull << q);
-      }
-      ok = __syncthreads_and(ok);
-      if (!ok) break;
-      if (any_fix) {
-        for (int s2 = first_new; s2 < need_hi; s2++)
-          if (loaded(s2)) fixup_plane(ring + size_t((s2 + H) % NR) * PLANE);
-        __syncthreads();
-      }
-      if (tid == 0) produce(lo - H + NR);
-
-      const int za = fwd ? z0 + lo : z1 - hi;
-      const int nz = hi - lo;
-      // Rolling window over planes za-H .. za+nz-1+H.
-      constexpr int WCOL = Cf::BOX ? WC : V;
-      constexpr int WROW = Cf::BOX ? WR : RY;
-      T win[NW][WROW][WCOL];
-      auto load_plane = [&](T (&dst)[WROW][WCOL], int z) {
-        const T* sl = slot_of(z);
-#pragma unroll
-        for (int r = 0; r < WROW; r++) {
-          const T* row = sl + (cy + r + (Cf::BOX ? 0 : H)) * RWX + HP + cx;
-          VT v = *reinterpret_cast<const VT*>(row);
-          const T* ve = reinterpret_cast<const T*>(&v);
-          if constexpr (Cf::BOX) {
-#pragma unroll
-            for (int e = 0; e < V; e++) dst[r][H + e] = ve[e];
-#pragma unroll
-            for (int k = 1; k <= H; k++) {
-              dst[r][H - k] = row[-k];
-              dst[r][H + V - 1 + k] = row[V - 1 + k];
+      if (producer) {
+        // one row: columns [x0-HP, x0+SW+HP) clipped to [0, px)
+        const int src_lo = max(x0 - HP, 0), src_hi = min(x0 + SW + HP, px);
+        const int dst_off = src_lo - (x0 - HP);
+        const unsigned row_bytes = unsigned(src_hi - src_lo) * unsigned(sizeof(T));
+        const int ry_lo = max(y0 - H, 0), ry_hi = min(y0 + TY + H, wy);
+        const unsigned plane_bytes = row_bytes * unsigned(ry_hi - ry_lo);
+        for (int q = -H; q < ZN + H; q++) {
+          const int s = slot_index(q);
+          if (pc + H + q >= NR) {  // wait until every compute warp released the slot's previous plane
+            bool w = mbar_wait(&empty[s], slot_parity(q) ^ 1u);
+            w = __all_sync(0xffffffffu, w);
+            if (!w) {
+              if (lane == 0) atomicOr(p.status, kErrCopyTimeout);
+              ok = false;
+              break;
             }
-          } else {
-#pragma unroll
-            for (int e = 0; e < V; e++) dst[r][e] = ve[e];
           }
+          const int z = fwd ? z_lo + q : z_hi - 1 - q;
+          const bool in = z >= 0 && z < h;
+          if (lane == 0) mbar_arrive_expect_tx(&full[s], in ? plane_bytes : 0u);
+          __syncwarp();
+          if (in) {
+            T* dst = ring + size_t(s) * PLANE + dst_off;
+            const T* src = fin + size_t(z) * wy * px + src_lo;
+            for (int r = ry_lo + lane; r < ry_hi; r += 32)
+              bulk_g2s(dst + (r - (y0 - H)) * RWX, src + size_t(r) * px, row_bytes, &full[s], pol);
+          }
+          issued = pc + H + q + 1;
         }
-      };
+      } else {
+        // Lane layout: vector k (V16 elements, 16 bytes) of a lane holds tile
+        // columns k*32*V16 + lane*V16 + [0, V16), so every warp-wide 16-byte
+        // access is one contiguous 512-byte run (no bank conflicts).
+        const bool ghost = !dir && x0 + SW > wx;  // columns past the domain inside the tile
+        const int lw = wx - 1 - x0;               // tile-local last column
+        const int lw_i = min(lw / (32 * V16), NV - 1) * V16 + lw % V16;  // its element index
+        const int lw_lane = (lw / V16) & 31;                              // and lane
+        auto col = [&](int i) { return (i / V16) * (32 * V16) + lane * V16 + i % V16; };
+        auto plane_ptr = [&](int z) -> const T* {
+          const int zc = min(max(z, 0), h - 1);
+          const int q = fwd ? zc - z_lo : z_hi - 1 - zc;
+          return ring + size_t(slot_index(q)) * PLANE + HP;
+        };
+        auto row_ptr = [&](const T* plane, int y) -> const T* {
+          const int yc = min(max(y, 0), wy - 1);
+          return plane + (yc - (y0 - H)) * RWX;
+        };
+        // this lane's V values of a row; in a ghost tile columns past the
+        // domain take the value of column wx-1
+        auto load_vals = [&](const T* row, T(&v)[V]) {
 #pragma unroll
-      for (int j = 0; j < 2 * H; j++) load_plane(win[j], za - H + j);
+          for (int k = 0; k < NV; k++) vec16_load(row + k * 32 * V16 + lane * V16, v + k * V16);
+          if (ghost) {
+            T edge = v[0];
 #pragma unroll
-      for (int k = 0; k < R; k++) {
-        if (k < nz) {
-          const int z = za + k;
-          load_plane(win[(k + 2 * H) % NW], z + H);
-          // star shapes: cross window of the centre plane
-          T cr[Cf::BOX ? 1 : WR][Cf::BOX ? 1 : WC];
-          if constexpr (!Cf::BOX) {
-            const T* sl = slot_of(z);
+            for (int i = 1; i < V; i++) edge = (lw_i == i) ? v[i] : edge;
+            edge = __shfl_sync(0xffffffffu, edge, lw_lane);
 #pragma unroll
-            for (int r = 0; r < WR; r++) {
-              const T* row = sl + (cy + r) * RWX + HP + cx;
-              if (r >= H && r < H + RY) {
-                VT v = *reinterpret_cast<const VT*>(row);
-                const T* ve = reinterpret_cast<const T*>(&v);
+            for (int i = 0; i < V; i++) v[i] = (col(i) > lw) ? edge : v[i];
+          }
+        };
+        // per vector: its V16 values with H neighbours on each side. A lane
+        // sends the value its right (left) neighbour lane needs; lane 31 (0)
+        // sends from the previous (next) vector, which is what lane 0 (31)
+        // needs across the vector boundary. The tile's outer neighbours come
+        // from the slot's pad columns at the clamped column (every lane reads
+        // the same word: a broadcast).
+        auto hwin = [&](const T* row, const T(&v)[V], T(&w)[NV][WV]) {
 #pragma unroll
-                for (int e = 0; e < V; e++) cr[r][H + e] = ve[e];
+          for (int k = 0; k < NV; k++) {
 #pragma unroll
-                for (int kk = 1; kk <= H; kk++) {
-                  cr[r][H - kk] = row[-kk];
-                  cr[r][H + V - 1 + kk] = row[V - 1 + kk];
-                }
+            for (int e = 0; e < V16; e++) w[k][H + e] = v[k * V16 + e];
+#pragma unroll
+            for (int d = 1; d <= H; d++) {
+              const T give_l = (k > 0 && lane == 31) ? v[(k - 1) * V16 + V16 - d] : v[k * V16 + V16 - d];
+              const T give_r = (k + 1 < NV && lane == 0) ? v[(k + 1) * V16 + d - 1] : v[k * V16 + d - 1];
+              const T from_l = __shfl_sync(0xffffffffu, give_l, (lane + 31) & 31);
+              const T from_r = __shfl_sync(0xffffffffu, give_r, (lane + 1) & 31);
+              if (k == 0) {
+                const T pad = row[max(-d, -x0)];
+                w[k][H - d] = lane > 0 ? from_l : pad;
               } else {
-                VT v = *reinterpret_cast<const VT*>(row);
-                const T* ve = reinterpret_cast<const T*>(&v);
-#pragma unroll
-                for (int e = 0; e < V; e++) cr[r][H + e] = ve[e];
+                w[k][H - d] = from_l;
+              }
+              if (k == NV - 1) {
+                const T pad = row[min(SW + d - 1, lw)];
+                w[k][H + V16 - 1 + d] = lane < 31 ? from_r : pad;
+              } else {
+                w[k][H + V16 - 1 + d] = from_r;
               }
             }
           }
-#pragma unroll
-          for (int ry = 0; ry < RY; ry++) {
-            const int y = y0 + cy + ry;
-            T o[V];
-#pragma unroll
-            for (int e = 0; e < V; e++) {
-              auto u = [&](int dz, int dy, int dx) -> T {
-                if constexpr (Cf::BOX) {
-                  return win[(k + H + dz) % NW][ry + H + dy][H + e + dx];
-                } else {
-                  if (dz == 0) return cr[ry + H + dy][H + e + dx];
-                  return win[(k + H + dz) % NW][ry][e];
-                }
-              };
-              o[e] = stencil_point<T, SHAPE, FAST>(u);
-            }
-            if (p.dirichlet) {
-              const bool fixed = z < H || z >= h - H || y < H || y >= wy - H;
-#pragma unroll
-              for (int e = 0; e < V; e++) {
-                const int x = x0 + cx + e;
-                const T old = Cf::BOX ? win[(k + H) % NW][ry + H][H + e] : win[(k + H) % NW][ry][e];
-                if (fixed || x < H || x >= wx - H) o[e] = old;
-              }
-            }
-            VT ov;
-            T* oe = reinterpret_cast<T*>(&ov);
-#pragma unroll
-            for (int e = 0; e < V; e++) oe[e] = o[e];
-            const bool inside = (y < wy) && (x0 + cx < px);
-            if (is_res(z)) {
-              const int tz = fwd ? z - (R + H) : z + (R + H);
-              int s = (tz - zres0 + off) % M;
-              if (s < 0) s += M;
-              *reinterpret_cast<VT*>(res + size_t(s) * PLANE + (H + cy + ry) * RWX + HP + cx) = ov;
-              const bool edge = (cy + ry < H) || (cy + ry >= TY - H) || (cx < HP) || (cx >= TX - HP);
-              if (inside && edge) *reinterpret_cast<VT*>(fout + (size_t(z) * wy + y) * px + x0 + cx) = ov;
-            } else if (inside) {
-              *reinterpret_cast<VT*>(fout + (size_t(z) * wy + y) * px + x0 + cx) = ov;
+        };
+
+        int wq = -H;  // next segment position to wait for
+        for (int q = 0; q < ZN && ok; q++) {
+          for (; wq <= q + H; wq++) {
+            bool w = mbar_wait(&full[slot_index(wq)], slot_parity(wq));
+            w = __all_sync(0xffffffffu, w);
+            if (!w) {
+              if (lane == 0) atomicOr(p.status, kErrCopyTimeout);
+              ok = false;
+              break;
             }
           }
+          if (!ok) break;
+          const int z = fwd ? z_lo + q : z_hi - 1 - q;
+          const T* pl[NP];
+#pragma unroll
+          for (int j = 0; j < NP; j++) pl[j] = plane_ptr(z - H + j);
+          const bool zfix = z < H || z >= h - H;
+          const int yw = y0 + wid * RY;  // this warp's first row
+          // finish one output row: Dirichlet cells keep the old value, store
+          auto finish = [&](int y, T(&o)[V], const T(&c)[V]) {
+            if (dir) {
+              const bool fixed = zfix || y < H || y >= wy - H;
+#pragma unroll
+              for (int i = 0; i < V; i++) {
+                const int x = x0 + col(i);
+                o[i] = (fixed || x < H || x >= wx - H) ? c[i] : o[i];
+              }
+            }
+            if (y < wy) {
+              T* dst = fout + (size_t(z) * wy + y) * px + x0 + lane * V16;
+#pragma unroll
+              for (int k2 = 0; k2 < NV; k2++)
+                if (x0 + k2 * 32 * V16 + lane * V16 < px) vec16_store(dst + k2 * 32 * V16, o + k2 * V16);
+            }
+          };
+          if constexpr (BOX) {
+            // rows yw-1 .. yw+RY of the three planes, three at a time
+            T bw[3][3][NV][WV];  // [plane][row % 3][vector][window]
+            auto bring = [&](int j) {  // row yw-1+j of every plane into bw[.][j % 3]
+#pragma unroll
+              for (int dz = 0; dz < 3; dz++) {
+                const T* row = row_ptr(pl[dz], yw - 1 + j);
+                T v[V];
+                load_vals(row, v);
+                hwin(row, v, bw[dz][j % 3]);
+              }
+            };
+            bring(0);
+            bring(1);
+            static_for<RY>([&](auto ryc) {
+              constexpr int ry = decltype(ryc)::value;
+              bring(ry + 2);
+              T o[V], c[V];
+#pragma unroll
+              for (int i = 0; i < V; i++) {
+                const int kk = i / V16, e = i % V16;
+                auto u = [&](int dz, int dy, int dx) -> T { return bw[dz + 1][(ry + 1 + dy) % 3][kk][H + e + dx]; };
+                o[i] = stencil_point<T, SHAPE, FAST>(u);
+                c[i] = bw[1][(ry + 1) % 3][kk][H + e];
+              }
+              finish(yw + ry, o, c);
+            });
+          } else {
+            constexpr int NC = 2 * H + 1;
+            T cr[NC][V];  // rolling rows of the centre plane: row yw-H+j in cr[j % NC]
+            static_for<2 * H>([&](auto jc) {
+              constexpr int j = decltype(jc)::value;
+              load_vals(row_ptr(pl[H], yw - H + j), cr[j]);
+            });
+            static_for<RY>([&](auto ryc) {
+              constexpr int ry = decltype(ryc)::value;
+              const int y = yw + ry;
+              load_vals(row_ptr(pl[H], y + H), cr[(ry + 2 * H) % NC]);
+              T cen[NV][WV];
+              hwin(row_ptr(pl[H], y), cr[(ry + H) % NC], cen);
+              T nz[2 * H][V];  // row y of planes z-H..z-1 then z+1..z+H
+#pragma unroll
+              for (int d = 1; d <= H; d++) {
+                load_vals(row_ptr(pl[H - d], y), nz[H - d]);
+                load_vals(row_ptr(pl[H + d], y), nz[H + d - 1]);
+              }
+              T o[V], c[V];
+#pragma unroll
+              for (int i = 0; i < V; i++) {
+                const int kk = i / V16, e = i % V16;
+                auto u = [&](int dz, int dy, int dx) -> T {
+                  if (dz != 0) return nz[dz < 0 ? H + dz : H + dz - 1][i];
+                  if (dy != 0) return cr[(ry + H + dy) % NC][i];
+                  return cen[kk][H + e + dx];
+                };
+                o[i] = stencil_point<T, SHAPE, FAST>(u);
+                c[i] = cen[kk][H + e];
+              }
+              finish(y, o, c);
+            });
+          }
+          // plane at position q-H is not read by later outputs
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&empty[slot_index(q - H)]);
+        }
+        if (ok) {  // the segment's last 2H positions are released without an output
+          __syncwarp();
+          if (lane == 0)
+            for (int q = ZN - H; q < ZN + H; q++) mbar_arrive(&empty[slot_index(q)]);
         }
       }
+      pc += ZN + 2 * H;
     }
-    }  // tile loop
-    if (ok && ntiles > int(gridDim.x)) {
-      set_tile(blockIdx.x);
-      tmx = x0 - HP;
-      tmy = y0 - H;
-    }
-    if (!ok) break;
-    if (M > 0) {
-      off = fwd ? off - (R + H) : off + (R + H);
-      off %= M;
-      if (off < 0) off += M;
-    }
-    if (it + 1 < p.steps) {
+    if (it + 1 < p.steps && p.persistent) {
       fence_proxy_async_global();
-      if (p.persistent) {
-        if (!gbar.sync()) { ok = false; break; }
-      }
+      if (!gbar.sync()) ok = false;
     }
   }
-  if (ok && C > 0) {
-    __syncthreads();
-    T* fnew = static_cast<T*>(p.f[(p.t0 + p.steps) & 1]);
-    for (int k = 0; k < C; k++) {
-      const int z = zres0 + k;
-      const T* sl = slot_of_res(z);
-#pragma unroll
-      for (int ry = 0; ry < RY; ry++) {
-        const int y = y0 + cy + ry;
-        if (y < wy && x0 + cx < px)
-          *reinterpret_cast<VT*>(fnew + (size_t(z) * wy + y) * px + x0 + cx) =
-              *reinterpret_cast<const VT*>(sl + (H + cy + ry) * RWX + HP + cx);
-      }
-    }
-  }
-  if (!ok) {
-    __syncthreads();
-    if (tid == 0) {
-      uint64_t ph = phase;
-      for (int s = waited; s < issued; s++) {
-        const int z = fwd ? z0 + s : z1 - 1 - s;
-        if (z < 0 || z >= h || (C > 0 && z >= zres0 && z < zres0 + C)) continue;
-        const int q = (s + H) % NR;
-        long long tw = clock64();
-        while (!mbar_try_wait(&bars[q], unsigned(ph >> q) & 1u)) {
-          if (clock64() - tw > (1ll << 28)) break;
-        }
-        ph ^= (1ull << q);
+  if (!ok && producer && lane == 0) {
+    // leave no bulk copy in flight into this CTA's shared memory: the last NR
+    // issued positions are the only ones whose copies may still be running
+    for (long long P = max(0ll, issued - NR); P < issued; P++) {
+      const int s = int(P % NR);
+      const unsigned par = unsigned((P / NR) & 1);
+      const long long t0 = clock64();
+      while (!mbar_try_wait(&full[s], par)) {
+        if (clock64() - t0 > (1ll << 30)) break;
       }
     }
   }

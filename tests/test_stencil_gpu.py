@@ -83,7 +83,9 @@ def test_2d_resident_rows_are_used(native, cuda, oracle):
 
 
 CASES_3D = [((1, 1, 1), 0, 2), ((3, 5, 7), 0, 3), ((17, 33, 70), 0, 4), ((40, 70, 130), 4, 5),
-            ((64, 40, 66), 2, 6), ((9, 100, 200), 0, 3)]
+            ((64, 40, 66), 2, 6), ((9, 100, 200), 0, 3),
+            # widths one or two columns past a tile edge (64/128/256-column tiles)
+            ((6, 40, 257), 5, 3), ((4, 33, 129), 3, 3), ((4, 20, 65), 2, 4), ((3, 9, 258), 0, 3)]
 
 
 @pytest.mark.parametrize("shape", SHAPES3D)
@@ -101,14 +103,15 @@ def test_3d_ragged_vs_oracle(native, cuda, oracle, shape, dt):
 
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
 @pytest.mark.parametrize("shape", ["3d7pt", "3d13pt", "3d27pt"])
-def test_3d_resident_planes_are_used(native, cuda, oracle, dt, shape):
-    # 2x3 (f32) / 2x3 (f64) x-y tiles, one slab per tile: every CTA keeps planes
-    f = np.random.default_rng(4).random((64, 40, 66)).astype(dt)
-    ctas = 2 * ((40 + 31) // 32) if dt == np.float32 else 2 * ((40 + 15) // 16)
-    for l2 in (False, True):
-        g, st = run(native, cuda, f, shape, 6, ctas=ctas, l2_sweep=l2)
-        assert st["cached_rows"] > 0
-        assert bits_equal(g, oracle.stencil(shape, f, 6)), (shape, dt, l2)
+def test_3d_work_split(native, cuda, oracle, dt, shape):
+    # Every CTA takes an equal run of (tile, plane) pairs: runs that start and
+    # end inside tiles, span two tiles, or are shorter than the stencil's reach.
+    f = np.random.default_rng(4).random((37, 70, 300)).astype(dt)
+    ref = oracle.stencil(shape, f, 4)
+    for ctas in (1, 3, 7, 13, 50, 152):
+        for l2 in (False, True):
+            g, st = run(native, cuda, f, shape, 4, ctas=ctas, l2_sweep=l2)
+            assert bits_equal(g, ref), (shape, dt, ctas, l2)
 
 
 @pytest.mark.parametrize("shape", ["2d5pt", "2ds25pt", "2d25pt", "3d7pt", "3d27pt", "poisson"])
