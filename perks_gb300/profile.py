@@ -1,0 +1,76 @@
+"""One short, self-contained launch of a hot-path kernel, for profilers.
+
+  python -m perks_gb300.profile stencil --shape 3d27pt --dims 256,256,256 --dtype f32 --order fast --steps 3
+  python -m perks_gb300.profile cg --matrix lap2d --n 512 --dtype fp64 --iters 20
+
+Runs one warm-up call, then exactly one call of the requested size, and
+prints its stats as one JSON line. The warm-up uses the same kernel with 2
+time steps (stencil) or 2 iterations (CG), so an ncu filter of
+`-k regex:<kernel> -s 1 -c 1` captures the second call. Fields are seeded
+uniform [0,1); CG right-hand sides uniform [-1,1).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+
+
+def _stencil(a):
+    import torch
+    from . import stencil as S
+    dims = tuple(int(x) for x in a.dims.split(","))
+    dt = {"f32": torch.float32, "f64": torch.float64}[a.dtype]
+    g = torch.Generator(device="cpu").manual_seed(1)
+    d = torch.rand(dims, generator=g, dtype=dt).cuda()
+    o = torch.empty_like(d)
+    kw = dict(kernel=a.kernel, order=a.order, l2_sweep=a.l2_sweep)
+    fn = S.stencil2d if len(dims) == 2 else S.stencil3d
+    fn(d, a.shape, 2, out=o, **kw)
+    torch.cuda.synchronize()
+    _, st = fn(d, a.shape, a.steps, out=o, **kw)
+    torch.cuda.synchronize()
+    return {"shape": a.shape, "dims": dims, "dtype": a.dtype, "order": a.order, "steps": a.steps, **st}
+
+
+def _cg(a):
+    import numpy as np
+    from . import cg as C
+    from . import matrices as M
+    rp, ci, v = M.laplacian_2d(a.n) if a.matrix == "lap2d" else M.laplacian_3d(a.n)
+    b = np.random.default_rng(1).uniform(-1, 1, len(rp) - 1)
+    kw = dict(dtype=a.dtype, tol=0.0, static_iter=True, check=False)
+    if a.format == "dia":
+        off, data = M.csr_to_dia(rp, ci, v)
+        C.cg_dia(off, data, b, max_iter=2, **kw)
+        _, res = C.cg_dia(off, data, b, max_iter=a.iters, **kw)
+    else:
+        C.cg_csr(rp, ci, v, b, max_iter=2, **kw)
+        _, res = C.cg_csr(rp, ci, v, b, max_iter=a.iters, **kw)
+    return {"matrix": a.matrix, "n": a.n, "format": a.format, "dtype": a.dtype, **res}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m perks_gb300.profile")
+    sub = ap.add_subparsers(dest="what", required=True)
+    s = sub.add_parser("stencil")
+    s.add_argument("--shape", required=True)
+    s.add_argument("--dims", required=True, help="wy,wx or h,wy,wx")
+    s.add_argument("--dtype", default="f32", choices=["f32", "f64"])
+    s.add_argument("--order", default="reference", choices=["reference", "fast"])
+    s.add_argument("--kernel", default="persistent", choices=["persistent", "per_step"])
+    s.add_argument("--l2-sweep", action="store_true")
+    s.add_argument("--steps", type=int, default=3)
+    c = sub.add_parser("cg")
+    c.add_argument("--matrix", default="lap2d", choices=["lap2d", "lap3d"])
+    c.add_argument("--n", type=int, default=512, help="grid points per dimension")
+    c.add_argument("--format", default="csr", choices=["csr", "dia"])
+    c.add_argument("--dtype", default="fp64", choices=["fp64", "fp32", "mixed"])
+    c.add_argument("--iters", type=int, default=20)
+    a = ap.parse_args(argv)
+    out = _stencil(a) if a.what == "stencil" else _cg(a)
+    print(json.dumps(out, default=str), flush=True)
+
+
+if __name__ == "__main__":
+    sys.exit(main())
