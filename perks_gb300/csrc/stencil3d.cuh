@@ -8,10 +8,15 @@
 //   gridDim.x equal ranges; CTA b sweeps its range every step as one or two
 //   z-runs ("segments") of one tile each, so every SM gets the same number of
 //   cells whatever the domain's shape.
-//   A CTA has NWC compute warps and one producer warp. The producer copies
-//   each input plane of a segment (TY + 2H rows of SW + 2HP columns, one
-//   cp.async.bulk per row, spread over its lanes, clipped to the field) into a
-//   ring of NR shared-memory slots and completes the slot's "full" mbarrier.
+//   A CTA has NWC compute warps and one producer warp. For each input plane
+//   of a segment the producer issues three tiled TMA copies into one of NR
+//   shared-memory ring slots: the tile's TY + 2H rows of SW columns, and the
+//   HP columns left and right of it as two separate strips (a box is at most
+//   256 elements wide; the strips keep every destination 128-byte aligned).
+//   Coordinates outside the field read as zero and are never used: the
+//   consumers clamp every index. The copies complete the slot's "full"
+//   mbarrier. (One cp.async.bulk per row costs about 100 SM cycles of copy
+//   issue each, which capped the kernel at ~2.9G rows/s.)
 //   Compute warp w owns RY rows of the tile: for output plane z it reads
 //   planes z-H..z+H from the ring, keeps a rolling window of rows in
 //   registers, moves horizontal neighbours between lanes by shuffles, writes
@@ -26,6 +31,7 @@
 // clamped), or Dirichlet (outer H cells keep their input value). Rows and
 // planes outside the domain are never copied.
 #pragma once
+#include <cuda.h>
 #include <cstdint>
 #include <type_traits>
 #include "ptx.cuh"
@@ -52,7 +58,18 @@ __device__ __forceinline__ void vec16_store(T* dst, const T* src) {
     *reinterpret_cast<double2*>(dst) = make_double2(src[0], src[1]);
 }
 
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar,
+                                            uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cta.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint"
+      " [%0], [%1, {%2, %3, %4}], [%5], %6;" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
+}
+
 struct Stencil3DParams {
+  CUtensorMap map[2];   // box {SW, TY+2H, 1} over field 0 / 1
+  CUtensorMap pmap[2];  // box {HP, TY+2H, 1}: the pad strips
   void* f[2];
   int h, wy, wx, px;  // domain and x pitch (elements)
   int gx, gy;         // x-y tile grid
@@ -71,16 +88,21 @@ struct Cfg3D {
   static constexpr int V = NV * V16;                      // columns per lane
   static constexpr int SW = 32 * V;                       // tile width
   static constexpr int HP = ((H + V16 - 1) / V16) * V16;  // pad columns each side (16-byte multiple)
-  // 8 compute warps + the producer: 9 warps leave 168 registers per thread
-  // (3 warps on the fullest SM sub-partition), enough for every window here
-  static constexpr int NWC = 8;
-  static constexpr int RY = 4;                            // rows per compute warp
+  // Compute warps and rows per warp. FP32: 15 + the producer = 16 warps, 4 per
+  // SM sub-partition, 128 registers per thread; the kernel is latency-bound,
+  // so warps matter more than rows. FP64 is bound by the FP64 pipe: 8 + 1
+  // warps (168 registers) keep its larger windows out of local memory.
+  static constexpr int NWC = sizeof(T) == 4 ? 15 : 8;
+  static constexpr int RY = sizeof(T) == 4 ? 2 : 4;       // rows per compute warp
   static constexpr int TY = NWC * RY;                     // tile height
   static constexpr int NT = (NWC + 1) * 32;
-  static constexpr int RWX = SW + 2 * HP;                 // slot row width
   static constexpr int SR = TY + 2 * H;                   // slot rows
   static constexpr int AL = 128 / sizeof(T);
-  static constexpr int PLANE = ((SR * RWX + AL - 1) / AL) * AL;  // slot stride (elements)
+  // slot: [SR][SW] tile rows, then [SR][HP] left pad, then [SR][HP] right pad
+  static constexpr int MAIN = ((SR * SW + AL - 1) / AL) * AL;
+  static constexpr int PADSZ = ((SR * HP + AL - 1) / AL) * AL;
+  static constexpr int PLANE = MAIN + 2 * PADSZ;           // slot stride (elements)
+  static constexpr unsigned tx_bytes = unsigned((SR * SW + 2 * SR * HP) * sizeof(T));
   static constexpr size_t slot_bytes = size_t(PLANE) * sizeof(T);
   // planes in flight beyond the 2H+1 being read: about 72 KB, at least 2,
   // within a 200 KB ring
@@ -94,6 +116,7 @@ struct Cfg3D {
   static constexpr size_t smem_bytes = ring_bytes + 2 * NR * sizeof(uint64_t);
   static_assert(D >= 1, "ring too small");
   static_assert(H <= V16, "horizontal neighbours are at most one lane away");
+  static_assert(SW <= 256 && SR <= 256, "TMA box extent");
 };
 
 template <class T, int SHAPE, bool FAST>
@@ -101,7 +124,7 @@ __global__ void __launch_bounds__(Cfg3D<T, SHAPE>::NT, 1)
     stencil3d_kernel(const __grid_constant__ Stencil3DParams p) {
   using Cf = Cfg3D<T, SHAPE>;
   constexpr int H = Cf::H, V = Cf::V, V16 = Cf::V16, NV = Cf::NV, SW = Cf::SW, HP = Cf::HP, RY = Cf::RY,
-                NWC = Cf::NWC, TY = Cf::TY, RWX = Cf::RWX, PLANE = Cf::PLANE, NR = Cf::NR;
+                NWC = Cf::NWC, TY = Cf::TY, PLANE = Cf::PLANE, NR = Cf::NR, MAIN = Cf::MAIN, PADSZ = Cf::PADSZ;
   constexpr bool BOX = Cf::BOX;
   constexpr int WV = V16 + 2 * H;  // horizontal window of one vector
   constexpr int NP = 2 * H + 1;    // planes one output reads
@@ -157,12 +180,6 @@ __global__ void __launch_bounds__(Cfg3D<T, SHAPE>::NT, 1)
       auto slot_parity = [&](int q) { return (par0 + unsigned((sb + q + NR) / NR)) & 1u; };
 
       if (producer) {
-        // one row: columns [x0-HP, x0+SW+HP) clipped to [0, px)
-        const int src_lo = max(x0 - HP, 0), src_hi = min(x0 + SW + HP, px);
-        const int dst_off = src_lo - (x0 - HP);
-        const unsigned row_bytes = unsigned(src_hi - src_lo) * unsigned(sizeof(T));
-        const int ry_lo = max(y0 - H, 0), ry_hi = min(y0 + TY + H, wy);
-        const unsigned plane_bytes = row_bytes * unsigned(ry_hi - ry_lo);
         for (int q = -H; q < ZN + H; q++) {
           const int s = slot_index(q);
           if (pc + H + q >= NR) {  // wait until every compute warp released the slot's previous plane
@@ -175,15 +192,18 @@ __global__ void __launch_bounds__(Cfg3D<T, SHAPE>::NT, 1)
             }
           }
           const int z = fwd ? z_lo + q : z_hi - 1 - q;
-          const bool in = z >= 0 && z < h;
-          if (lane == 0) mbar_arrive_expect_tx(&full[s], in ? plane_bytes : 0u);
-          __syncwarp();
-          if (in) {
-            T* dst = ring + size_t(s) * PLANE + dst_off;
-            const T* src = fin + size_t(z) * wy * px + src_lo;
-            for (int r = ry_lo + lane; r < ry_hi; r += 32)
-              bulk_g2s(dst + (r - (y0 - H)) * RWX, src + size_t(r) * px, row_bytes, &full[s], pol);
+          if (lane == 0) {
+            if (z >= 0 && z < h) {
+              T* slot = ring + size_t(s) * PLANE;
+              mbar_arrive_expect_tx(&full[s], Cf::tx_bytes);
+              tma_load_3d(slot, &p.map[t & 1], x0, y0 - H, z, &full[s], pol);
+              tma_load_3d(slot + MAIN, &p.pmap[t & 1], x0 - HP, y0 - H, z, &full[s], pol);
+              tma_load_3d(slot + MAIN + PADSZ, &p.pmap[t & 1], x0 + SW, y0 - H, z, &full[s], pol);
+            } else {
+              mbar_arrive_expect_tx(&full[s], 0u);  // a plane outside the domain: never read
+            }
           }
+          __syncwarp();
           issued = pc + H + q + 1;
         }
       } else {
@@ -198,15 +218,20 @@ __global__ void __launch_bounds__(Cfg3D<T, SHAPE>::NT, 1)
         auto plane_ptr = [&](int z) -> const T* {
           const int zc = min(max(z, 0), h - 1);
           const int q = fwd ? zc - z_lo : z_hi - 1 - zc;
-          return ring + size_t(slot_index(q)) * PLANE + HP;
+          return ring + size_t(slot_index(q)) * PLANE;
         };
-        auto row_ptr = [&](const T* plane, int y) -> const T* {
-          const int yc = min(max(y, 0), wy - 1);
-          return plane + (yc - (y0 - H)) * RWX;
+        // a row of a slot: its index there (clamped to the domain)
+        struct RowRef {
+          const T* plane;
+          int ri;
+        };
+        auto row_ref = [&](const T* plane, int y) -> RowRef {
+          return RowRef{plane, min(max(y, 0), wy - 1) - (y0 - H)};
         };
         // this lane's V values of a row; in a ghost tile columns past the
         // domain take the value of column wx-1
-        auto load_vals = [&](const T* row, T(&v)[V]) {
+        auto load_vals = [&](RowRef rw, T(&v)[V]) {
+          const T* row = rw.plane + rw.ri * SW;
 #pragma unroll
           for (int k = 0; k < NV; k++) vec16_load(row + k * 32 * V16 + lane * V16, v + k * V16);
           if (ghost) {
@@ -221,10 +246,13 @@ __global__ void __launch_bounds__(Cfg3D<T, SHAPE>::NT, 1)
         // per vector: its V16 values with H neighbours on each side. A lane
         // sends the value its right (left) neighbour lane needs; lane 31 (0)
         // sends from the previous (next) vector, which is what lane 0 (31)
-        // needs across the vector boundary. The tile's outer neighbours come
-        // from the slot's pad columns at the clamped column (every lane reads
-        // the same word: a broadcast).
-        auto hwin = [&](const T* row, const T(&v)[V], T(&w)[NV][WV]) {
+        // needs across the vector boundary. The tile's outer neighbours are
+        // read at the clamped column from the tile row or a pad strip (every
+        // lane reads the same word: a broadcast).
+        auto hwin = [&](RowRef rw, const T(&v)[V], T(&w)[NV][WV]) {
+          const T* row = rw.plane + rw.ri * SW;
+          const T* padl = rw.plane + MAIN + rw.ri * HP;
+          const T* padr = rw.plane + MAIN + PADSZ + rw.ri * HP;
 #pragma unroll
           for (int k = 0; k < NV; k++) {
 #pragma unroll
@@ -236,13 +264,14 @@ __global__ void __launch_bounds__(Cfg3D<T, SHAPE>::NT, 1)
               const T from_l = __shfl_sync(0xffffffffu, give_l, (lane + 31) & 31);
               const T from_r = __shfl_sync(0xffffffffu, give_r, (lane + 1) & 31);
               if (k == 0) {
-                const T pad = row[max(-d, -x0)];
+                const T pad = *(x0 == 0 ? row : padl + HP - d);  // column max(x0-d, 0)
                 w[k][H - d] = lane > 0 ? from_l : pad;
               } else {
                 w[k][H - d] = from_l;
               }
               if (k == NV - 1) {
-                const T pad = row[min(SW + d - 1, lw)];
+                const int c = min(SW + d - 1, lw);  // tile-local column min(x0+SW+d-1, wx-1)
+                const T pad = *(c < SW ? row + c : padr + (c - SW));
                 w[k][H + V16 - 1 + d] = lane < 31 ? from_r : pad;
               } else {
                 w[k][H + V16 - 1 + d] = from_r;
@@ -292,10 +321,10 @@ __global__ void __launch_bounds__(Cfg3D<T, SHAPE>::NT, 1)
             auto bring = [&](int j) {  // row yw-1+j of every plane into bw[.][j % 3]
 #pragma unroll
               for (int dz = 0; dz < 3; dz++) {
-                const T* row = row_ptr(pl[dz], yw - 1 + j);
+                const RowRef rw = row_ref(pl[dz], yw - 1 + j);
                 T v[V];
-                load_vals(row, v);
-                hwin(row, v, bw[dz][j % 3]);
+                load_vals(rw, v);
+                hwin(rw, v, bw[dz][j % 3]);
               }
             };
             bring(0);
@@ -318,19 +347,19 @@ __global__ void __launch_bounds__(Cfg3D<T, SHAPE>::NT, 1)
             T cr[NC][V];  // rolling rows of the centre plane: row yw-H+j in cr[j % NC]
             static_for<2 * H>([&](auto jc) {
               constexpr int j = decltype(jc)::value;
-              load_vals(row_ptr(pl[H], yw - H + j), cr[j]);
+              load_vals(row_ref(pl[H], yw - H + j), cr[j]);
             });
             static_for<RY>([&](auto ryc) {
               constexpr int ry = decltype(ryc)::value;
               const int y = yw + ry;
-              load_vals(row_ptr(pl[H], y + H), cr[(ry + 2 * H) % NC]);
+              load_vals(row_ref(pl[H], y + H), cr[(ry + 2 * H) % NC]);
               T cen[NV][WV];
-              hwin(row_ptr(pl[H], y), cr[(ry + H) % NC], cen);
+              hwin(row_ref(pl[H], y), cr[(ry + H) % NC], cen);
               T nz[2 * H][V];  // row y of planes z-H..z-1 then z+1..z+H
 #pragma unroll
               for (int d = 1; d <= H; d++) {
-                load_vals(row_ptr(pl[H - d], y), nz[H - d]);
-                load_vals(row_ptr(pl[H + d], y), nz[H + d - 1]);
+                load_vals(row_ref(pl[H - d], y), nz[H - d]);
+                load_vals(row_ref(pl[H + d], y), nz[H + d - 1]);
               }
               T o[V], c[V];
 #pragma unroll

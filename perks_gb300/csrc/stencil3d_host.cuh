@@ -1,5 +1,5 @@
-// Host launcher for the 3D stencil kernel: tile grid, per-CTA work ranges,
-// cooperative (persistent) or one-launch-per-step execution.
+// Host launcher for the 3D stencil kernel: tensor maps, tile grid, per-CTA
+// work ranges, cooperative (persistent) or one-launch-per-step execution.
 #pragma once
 #include <algorithm>
 #include <string>
@@ -7,6 +7,8 @@
 #include "stencil3d.cuh"
 
 namespace perks {
+
+int encode_tiled_3d(CUtensorMap* map, bool f64, void* base, int wx, int wy, int h, int px, int box_x, int box_y);
 
 template <class T, int SHAPE, bool FAST>
 int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h, int wy, int wx, int steps,
@@ -52,6 +54,13 @@ int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h
                                size_t(h) * wy, cudaMemcpyDeviceToDevice, s));
 
   Stencil3DParams p{};
+  for (int i = 0; i < 2; i++) {
+    void* base = i ? static_cast<void*>(f1) : static_cast<void*>(f0);
+    if ((stt = encode_tiled_3d(&p.map[i], sizeof(T) == 8, base, wx, wy, h, px, Cf::SW, Cf::SR)) != PERKS_OK)
+      return stt;
+    if ((stt = encode_tiled_3d(&p.pmap[i], sizeof(T) == 8, base, wx, wy, h, px, Cf::HP, Cf::SR)) != PERKS_OK)
+      return stt;
+  }
   p.f[0] = f0;
   p.f[1] = f1;
   p.h = h;
