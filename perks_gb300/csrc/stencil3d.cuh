@@ -88,12 +88,14 @@ struct Cfg3D {
   static constexpr int V = NV * V16;                      // columns per lane
   static constexpr int SW = 32 * V;                       // tile width
   static constexpr int HP = ((H + V16 - 1) / V16) * V16;  // pad columns each side (16-byte multiple)
-  // Compute warps and rows per warp. FP32: 15 + the producer = 16 warps, 4 per
-  // SM sub-partition, 128 registers per thread; the kernel is latency-bound,
-  // so warps matter more than rows. FP64 is bound by the FP64 pipe: 8 + 1
-  // warps (168 registers) keep its larger windows out of local memory.
-  static constexpr int NWC = sizeof(T) == 4 ? 15 : 8;
-  static constexpr int RY = sizeof(T) == 4 ? 2 : 4;       // rows per compute warp
+  // Compute warps and rows per warp (one more warp is the producer), from
+  // timing FP32 variants at 512^3: the 7-point star does best with 8 warps of
+  // 4 rows, the radius-2 and box shapes with 11 warps of 3 rows (12 warps: 168
+  // registers per thread). FP64 is bound by the FP64 pipe: 8 warps of 4 rows
+  // keep its larger windows out of local memory.
+  static constexpr bool WIDE = sizeof(T) == 4 && (BOX || H >= 2);
+  static constexpr int NWC = WIDE ? 11 : 8;
+  static constexpr int RY = WIDE ? 3 : 4;                 // rows per compute warp
   static constexpr int TY = NWC * RY;                     // tile height
   static constexpr int NT = (NWC + 1) * 32;
   static constexpr int SR = TY + 2 * H;                   // slot rows
