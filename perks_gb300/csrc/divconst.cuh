@@ -25,16 +25,14 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include "f32x2.cuh"
 
 namespace perks {
 
+// The steps after q0, e and q1: the midpoint fix and the sign/non-finite
+// handling, for one element.
 template <int B>
-__device__ __forceinline__ float div_const(float x) {
-  constexpr float b = float(B);
-  const float r = __fdiv_rn(1.0f, b);  // folded to a constant
-  const float q0 = __fmul_rn(x, r);
-  const float e = __fmaf_rn(-q0, b, x);
-  float q1 = __fmaf_rn(e, r, q0);
+__device__ __forceinline__ float div_finish(float x, float q0, float e, float q1) {
   if constexpr ((B & 1) == 0) {
     constexpr float half = float(B / 2) * 0x1p-149f;  // b/2 subnormal steps
     const bool tie = fabsf(e) == half;
@@ -42,6 +40,34 @@ __device__ __forceinline__ float div_const(float x) {
     q1 = tie ? ((__float_as_uint(q0) & 1u) ? up : q0) : q1;
   }
   return isfinite(q0) ? copysignf(q1, x) : q0;
+}
+
+template <int B>
+__device__ __forceinline__ float div_const(float x) {
+  constexpr float b = float(B);
+  const float r = __fdiv_rn(1.0f, b);  // folded to a constant
+  const float q0 = __fmul_rn(x, r);
+  const float e = __fmaf_rn(-q0, b, x);
+  const float q1 = __fmaf_rn(e, r, q0);
+  return div_finish<B>(x, q0, e, q1);
+}
+
+// Two elements at once: the three rounding steps as packed FP32 pairs (each
+// half an IEEE round-to-nearest operation, so each element's result is the
+// one above), the finish per element.
+template <int B>
+__device__ __forceinline__ F2 div_const(F2 x) {
+  constexpr float b = float(B);
+  const float r = __fdiv_rn(1.0f, b);
+  const F2 q0 = RN<F2>::mul(x, F2(r));
+  const F2 e = RN<F2>::fma(q0, F2(-b), x);  // -q0*b + x, the negation exact
+  const F2 q1 = RN<F2>::fma(e, F2(r), q0);
+  float xa, xb, q0a, q0b, ea, eb, q1a, q1b;
+  x.unpack(xa, xb);
+  q0.unpack(q0a, q0b);
+  e.unpack(ea, eb);
+  q1.unpack(q1a, q1b);
+  return F2::pack(div_finish<B>(xa, q0a, ea, q1a), div_finish<B>(xb, q0b, eb, q1b));
 }
 
 template <int B>

@@ -46,8 +46,6 @@ PERKS_SHAPE_INFO(PERKS_POISSON, 1, true, true)
 #undef PERKS_SHAPE_INFO
 
 // Correctly rounded arithmetic that the compiler may not fuse.
-template <class T>
-struct RN;
 template <>
 struct RN<float> {
   static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
@@ -93,22 +91,33 @@ __host__ __device__ constexpr double c27(int z, int y, int x) {
 }
 
 // ------------------------------------------------------------ Ref order ----
+// 2D star, reference order: south (far to near), west (far to near), centre,
+// east, north, each term a rounded product added to the rounded running sum,
+// then / 118. `add(acc, p)` is the rounded sum (a packed-pair caller passes a
+// form ptxas cannot fuse with the product).
+template <class T, int SHAPE, class U, class Add>
+__device__ __forceinline__ T star2d_ref(const U& u, const Add& add) {
+  using O = RN<T>;
+  constexpr int H = ShapeInfo<SHAPE>::H;
+  T acc = O::mul(T(star_s(H - 1)), u(0, -H, 0));
+#pragma unroll
+  for (int h = H - 2; h >= 0; h--) acc = add(acc, O::mul(T(star_s(h)), u(0, -1 - h, 0)));
+#pragma unroll
+  for (int h = H - 1; h >= 0; h--) acc = add(acc, O::mul(T(star_w(h)), u(0, 0, -1 - h)));
+  acc = add(acc, O::mul(T(15), u(0, 0, 0)));
+#pragma unroll
+  for (int h = 0; h < H; h++) acc = add(acc, O::mul(T(star_e(h)), u(0, 0, 1 + h)));
+#pragma unroll
+  for (int h = 0; h < H; h++) acc = add(acc, O::mul(T(star_n(h)), u(0, 1 + h, 0)));
+  return div_const<118>(acc);
+}
+
 template <class T, int SHAPE, class U>
 __device__ __forceinline__ T point_ref(const U& u) {
   using O = RN<T>;
   constexpr int H = ShapeInfo<SHAPE>::H;
   if constexpr (SHAPE <= PERKS_2DS25PT) {
-    T acc = O::mul(T(star_s(H - 1)), u(0, -H, 0));
-#pragma unroll
-    for (int h = H - 2; h >= 0; h--) acc = O::add(acc, O::mul(T(star_s(h)), u(0, -1 - h, 0)));
-#pragma unroll
-    for (int h = H - 1; h >= 0; h--) acc = O::add(acc, O::mul(T(star_w(h)), u(0, 0, -1 - h)));
-    acc = O::add(acc, O::mul(T(15), u(0, 0, 0)));
-#pragma unroll
-    for (int h = 0; h < H; h++) acc = O::add(acc, O::mul(T(star_e(h)), u(0, 0, 1 + h)));
-#pragma unroll
-    for (int h = 0; h < H; h++) acc = O::add(acc, O::mul(T(star_n(h)), u(0, 1 + h, 0)));
-    return div_const<118>(acc);
+    return star2d_ref<T, SHAPE>(u, [](T a, T b) { return O::add(a, b); });
   } else if constexpr (SHAPE == PERKS_2D9PT || SHAPE == PERKS_2D25PT) {
     // Terms before the centre sum in T; the centre's double literal promotes
     // the rest of the sum to double; later products are still T products.
