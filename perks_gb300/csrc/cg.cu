@@ -6,8 +6,13 @@
 // stop test of the reference GPU kernel, conjugateGradient/cg_kernels.cuh:834):
 //   p = r (first) or p = r + beta p;  Ap = A p;  alpha = rr / p.Ap;
 //   x += alpha p;  r -= alpha Ap;  rr' = r.r;  beta = rr' / rr
-// Three grid barriers per iteration: after p (the SpMV gathers it), after
-// the p.Ap reduction, after the r.r reduction. Dot products are reduced
+// FP64: three grid barriers per iteration: after p (the SpMV gathers it),
+// after the p.Ap reduction, after the r.r reduction. FP32 and the FP32 inner
+// iteration of mixed precision form p on the fly in the SpMV gather instead
+// (p_j = beta*p_old_j + r_j, the same fma its owner applies, so the values are
+// identical) with p double-buffered, saving the p pass and one barrier; for
+// FP64 the extra fma per nonzero would cost more FP64 issue than it saves
+// (GB300 runs FP64 at 1/64 of FP32). Dot products are reduced
 // deterministically: each CTA writes one partial sum, and after the barrier
 // every CTA adds all partials in the same fixed order, so all CTAs derive
 // identical alpha / beta without atomics.
@@ -49,7 +54,7 @@ struct CgParams {
   const void* b;
   void* x;                // in: x0, out: solution (FP64 for FP64/mixed, FP32 for FP32)
   void* r;                // working vectors, working precision
-  void* p[2];             // p, double-buffered between iterations? (single buffer used; see below)
+  void* p[2];             // p; FP32 and mixed alternate the two buffers between iterations
   void* Ap;
   // mixed precision extras
   float* val32;           // FP32 copy of the matrix values (CSR nnz or DIA ndiag*n)
@@ -79,9 +84,10 @@ __device__ __forceinline__ int cg_split(const CgMat& A, int c, int ncta) {
   return lo;
 }
 
-template <class MV, class XV>
-__device__ __forceinline__ XV spmv_row(const CgMat& A, const MV* __restrict__ val, const XV* __restrict__ x, int i) {
-  // Accumulates in the working precision XV (double for FP64, float for FP32).
+// Row i of A times a vector given by xv(column). Accumulates in the working
+// precision XV (double for FP64, float for FP32).
+template <class XV, class MV, class XF>
+__device__ __forceinline__ XV spmv_row_f(const CgMat& A, const MV* __restrict__ val, const XF& xv, int i) {
   XV acc = XV(0);
   if (A.fmt == 0) {
     const int j0 = __ldg(A.rp + i), j1 = __ldg(A.rp + i + 1);
@@ -90,22 +96,26 @@ __device__ __forceinline__ XV spmv_row(const CgMat& A, const MV* __restrict__ va
     for (; j + 4 <= j1; j += 4) {
       const int c0 = __ldg(A.ci + j), c1 = __ldg(A.ci + j + 1), c2 = __ldg(A.ci + j + 2), c3 = __ldg(A.ci + j + 3);
       const XV v0 = XV(__ldg(val + j)), v1 = XV(__ldg(val + j + 1)), v2 = XV(__ldg(val + j + 2)), v3 = XV(__ldg(val + j + 3));
-      const XV x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
+      const XV x0 = xv(c0), x1 = xv(c1), x2 = xv(c2), x3 = xv(c3);
       acc = fma(v0, x0, acc);
       acc = fma(v1, x1, acc);
       acc = fma(v2, x2, acc);
       acc = fma(v3, x3, acc);
     }
-    for (; j < j1; j++) acc = fma(XV(__ldg(val + j)), x[__ldg(A.ci + j)], acc);
+    for (; j < j1; j++) acc = fma(XV(__ldg(val + j)), xv(__ldg(A.ci + j)), acc);
   } else {
 #pragma unroll 8
     for (int k = 0; k < A.ndiag; k++) {
       const int c = i + A.off[k];
       const XV a = XV(__ldg(val + (size_t)k * A.n + i));
-      if (c >= 0 && c < A.n) acc = fma(a, x[c], acc);
+      if (c >= 0 && c < A.n) acc = fma(a, xv(c), acc);
     }
   }
   return acc;
+}
+template <class MV, class XV>
+__device__ __forceinline__ XV spmv_row(const CgMat& A, const MV* __restrict__ val, const XV* __restrict__ x, int i) {
+  return spmv_row_f<XV>(A, val, [x](int c) { return x[c]; }, i);
 }
 
 // Block-wide sum of two doubles; result valid in every thread.
@@ -133,40 +143,75 @@ __device__ __forceinline__ void block_sum2(double& a, double& b) {
   }
 }
 
+// Block-wide sum of NV doubles, valid in thread 0 only: warps reduce by
+// shuffles, then warp 0 alone adds the warp sums (FP64 issue is scarce).
+template <int NV>
+__device__ __forceinline__ void block_sum_t0(double (&v)[NV]) {
+  __shared__ double sw[NV][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; k++)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  __syncthreads();  // the previous call's readers are done with sw
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; k++) sw[k][w] = v[k];
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+      v[k] = lane < nw ? sw[k][lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    }
+  }
+}
+
 // Grid-wide deterministic sum: every CTA stores its partials, one barrier,
 // then every CTA adds all partials in the same order.
 struct GridSum {
   double* part;  // [slot][2][gridDim]
   GridBarrier gb;
-  __device__ bool sum2(int slot, double& a, double& b) {
-    block_sum2(a, b);
+  template <int NV>
+  __device__ bool sum(int slot, double (&v)[NV]) {
+    block_sum_t0<NV>(v);
     const int G = gridDim.x;
     double* ps = part + size_t(slot) * 2 * G;
-    if (threadIdx.x == 0) {
-      ps[blockIdx.x] = a;
-      ps[G + blockIdx.x] = b;
-    }
-    if (!gb.sync()) return false;
-    __shared__ double ra, rb;
-    if (threadIdx.x < 32) {
-      double x = 0.0, y = 0.0;
-      for (int i = threadIdx.x; i < G; i += 32) {
-        x += __ldcg(ps + i);
-        y += __ldcg(ps + G + i);
-      }
+    if (threadIdx.x == 0)
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        x += __shfl_xor_sync(0xffffffffu, x, o);
-        y += __shfl_xor_sync(0xffffffffu, y, o);
-      }
-      if (threadIdx.x == 0) {
-        ra = x;
-        rb = y;
+      for (int k = 0; k < NV; k++) ps[k * G + blockIdx.x] = v[k];
+    if (!gb.sync()) return false;
+    __shared__ double rs[NV];
+    if (threadIdx.x < 32) {
+#pragma unroll
+      for (int k = 0; k < NV; k++) {
+        // independent loads, then a fixed-order sum
+        double acc = 0.0;
+#pragma unroll 8
+        for (int i = threadIdx.x; i < G; i += 32) acc += __ldcg(ps + k * G + i);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (threadIdx.x == 0) rs[k] = acc;
       }
     }
     __syncthreads();
-    a = ra;
-    b = rb;
+#pragma unroll
+    for (int k = 0; k < NV; k++) v[k] = rs[k];
+    return true;
+  }
+  __device__ bool sum2(int slot, double& a, double& b) {
+    double v[2] = {a, b};
+    if (!sum<2>(slot, v)) return false;
+    a = v[0];
+    b = v[1];
+    return true;
+  }
+  __device__ bool sum1(int slot, double& a) {
+    double v[1] = {a};
+    if (!sum<1>(slot, v)) return false;
+    a = v[0];
     return true;
   }
 };
@@ -187,12 +232,12 @@ constexpr int kU = 4;
 // build rounding of the scalars r.r, p.Ap, alpha and beta).
 template <class T>
 __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_constant__ CgParams P) {
+  constexpr bool FUSE = sizeof(T) == 4;  // p formed in the SpMV gather
   const CgMat& A = P.A;
   const T* __restrict__ val = static_cast<const T*>(A.val);
   const T* __restrict__ b = static_cast<const T*>(P.b);
   T* __restrict__ x = static_cast<T*>(P.x);
   T* __restrict__ r = static_cast<T*>(P.r);
-  T* __restrict__ p = static_cast<T*>(P.p[0]);
   T* __restrict__ Ap = static_cast<T*>(P.Ap);
   const int G = gridDim.x;
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
@@ -222,21 +267,45 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
       if (done) break;
     }
     if (k > P.max_iter) break;
-    if (k > 1) {
-      const T beta = r1 / r0;
-      CG_ROWS(i, { p[i] = fma(beta, p[i], r[i]); })
-    } else {
-      CG_ROWS(i, { p[i] = r[i]; })
-    }
-    if (!gs.gb.sync()) return;
+    T* __restrict__ p = static_cast<T*>(P.p[FUSE ? (k & 1) : 0]);
     T pap_t = T(0);
-    CG_ROWS(i, {
-      const T api = spmv_row(A, val, p, i);
-      Ap[i] = api;
-      pap_t = fma(p[i], api, pap_t);
-    })
-    double pap = double(pap_t), unused = 0.0;
-    if (!gs.sum2(1 + (k & 1), pap, unused)) return;
+    if constexpr (FUSE) {
+      // p = r (first) or beta p_old + r, formed where it is gathered
+      if (k > 1) {
+        const T beta = r1 / r0;
+        const T* __restrict__ po = static_cast<const T*>(P.p[(k + 1) & 1]);
+        CG_ROWS(i, {
+          const T api = spmv_row_f<T>(A, val, [&](int c) { return fma(beta, po[c], r[c]); }, i);
+          const T pi = fma(beta, po[i], r[i]);
+          p[i] = pi;
+          Ap[i] = api;
+          pap_t = fma(pi, api, pap_t);
+        })
+      } else {
+        CG_ROWS(i, {
+          const T api = spmv_row(A, val, static_cast<const T*>(r), i);
+          const T pi = r[i];
+          p[i] = pi;
+          Ap[i] = api;
+          pap_t = fma(pi, api, pap_t);
+        })
+      }
+    } else {
+      if (k > 1) {
+        const T beta = r1 / r0;
+        CG_ROWS(i, { p[i] = fma(beta, p[i], r[i]); })
+      } else {
+        CG_ROWS(i, { p[i] = r[i]; })
+      }
+      if (!gs.gb.sync()) return;
+      CG_ROWS(i, {
+        const T api = spmv_row(A, val, static_cast<const T*>(p), i);
+        Ap[i] = api;
+        pap_t = fma(p[i], api, pap_t);
+      })
+    }
+    double pap = double(pap_t);
+    if (!gs.sum1(1 + (k & 1), pap)) return;
     const T dot = T(pap);
     if (!(dot > T(0)) || !isfinite(double(dot))) {
       if (tid == 0 && blockIdx.x == 0) atomicOr(P.status, kErrBreakdown);
@@ -251,7 +320,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
       rrn_t = fma(ri, ri, rrn_t);
     })
     double rrn = double(rrn_t);
-    if (!gs.sum2(3, rrn, unused)) return;
+    if (!gs.sum1(3, rrn)) return;
     r0 = r1;
     r1 = T(rrn);
     k++;
@@ -273,7 +342,6 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
   double* __restrict__ x = static_cast<double*>(P.x);
   double* __restrict__ r64 = P.r64;
   float* __restrict__ r = static_cast<float*>(P.r);
-  float* __restrict__ p = static_cast<float*>(P.p[0]);
   float* __restrict__ Ap = static_cast<float*>(P.Ap);
   float* __restrict__ xs = P.xs;
   const int G = gridDim.x;
@@ -308,21 +376,31 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
   while (true) {
     if (!P.static_iter && rr < tol2) break;
     if (k > P.max_iter) break;
+    // p = r (first) or beta p_old + r, formed where it is gathered (the
+    // values its owner stores are the same fma)
+    float* __restrict__ p = static_cast<float*>(P.p[k & 1]);
+    float pap_t = 0.0f;
     if (k > 1) {
       const float beta = float(rr / rr0);
-      CG_ROWS(i, { p[i] = fmaf(beta, p[i], r[i]); })
+      const float* __restrict__ po = static_cast<const float*>(P.p[(k + 1) & 1]);
+      CG_ROWS(i, {
+        const float api = spmv_row_f<float>(A, val32, [&](int c) { return fmaf(beta, po[c], r[c]); }, i);
+        const float pi = fmaf(beta, po[i], r[i]);
+        p[i] = pi;
+        Ap[i] = api;
+        pap_t = fmaf(pi, api, pap_t);
+      })
     } else {
-      CG_ROWS(i, { p[i] = r[i]; })
+      CG_ROWS(i, {
+        const float api = spmv_row(A, val32, static_cast<const float*>(r), i);
+        const float pi = r[i];
+        p[i] = pi;
+        Ap[i] = api;
+        pap_t = fmaf(pi, api, pap_t);
+      })
     }
-    if (!gs.gb.sync()) return;
-    float pap_t = 0.0f;
-    CG_ROWS(i, {
-      const float api = spmv_row(A, val32, p, i);
-      Ap[i] = api;
-      pap_t = fmaf(p[i], api, pap_t);
-    })
-    double pap = double(pap_t), unused = 0.0;
-    if (!gs.sum2(1 + (k & 1), pap, unused)) return;
+    double pap = double(pap_t);
+    if (!gs.sum1(1 + (k & 1), pap)) return;
     if (!(pap > 0.0) || !isfinite(pap)) {
       if (tid == 0 && blockIdx.x == 0) atomicOr(P.status, kErrBreakdown);
       return;
@@ -336,7 +414,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       rrn_t = fmaf(ri, ri, rrn_t);
     })
     double rrn = double(rrn_t);
-    if (!gs.sum2(3, rrn, unused)) return;
+    if (!gs.sum1(3, rrn)) return;
     since++;
     const bool update = rrn < P.delta2 * maxrr || rrn < tol2 || (P.replace_every > 0 && since >= P.replace_every) ||
                         k == P.max_iter;
@@ -347,14 +425,14 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
         xs[i] = 0.0f;
       })
       if (!gs.gb.sync()) return;
-      double rt = 0.0, un2 = 0.0;
+      double rt = 0.0;
       CG_ROWS(i, {
         const double ri = b[i] - spmv_row(A, val64, x, i);
         r64[i] = ri;
         r[i] = float(ri);
         rt = fma(ri, ri, rt);
       })
-      if (!gs.sum2(0, rt, un2)) return;
+      if (!gs.sum1(0, rt)) return;
       rrn = rt;
       maxrr = rt;
       outer++;
@@ -553,7 +631,7 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   const size_t v64 = (size_t(n) * 8 + 255) & ~size_t(255);
   const size_t nval = A.fmt == 0 ? size_t(A.nnz) : size_t(A.ndiag) * n;
   constexpr size_t kTail = 80 * 1024;   // partial sums (4 slots x 2 x 1024 CTAs) + scalars
-  size_t need = 3 * vbytes + kTail;     // r, p, Ap + tail
+  size_t need = 4 * vbytes + kTail;     // r, p (two buffers), Ap + tail
   if (o->dtype == PERKS_MIXED) need += v64 + vbytes + ((nval * 4 + 255) & ~size_t(255));
   unsigned char* w = static_cast<unsigned char*>(workspace(kWsCgVec, need, &st));
   if (!w) return st;
@@ -565,9 +643,9 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   P.x = x;
   P.r = w;
   P.p[0] = w + vbytes;
-  P.p[1] = P.p[0];
+  P.p[1] = w + 3 * vbytes;
   P.Ap = w + 2 * vbytes;
-  unsigned char* tail = w + 3 * vbytes;
+  unsigned char* tail = w + 4 * vbytes;
   P.part = reinterpret_cast<double*>(tail);          // 4 slots x 2 x (<= 1024 CTAs)
   double* scal = P.part + 8 * 1024;                    // device scalars / results (32 doubles)
   unsigned char* more = tail + kTail;
