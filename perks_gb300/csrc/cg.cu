@@ -228,6 +228,37 @@ constexpr int kU = 4;
     }                                                                      \
   }
 
+// Streaming row loops: 4 consecutive rows per thread with 16-byte vector
+// accesses over the 4-aligned part of [row0, row1), the ragged ends (and
+// everything when `vec` is false, e.g. a caller's vector that is not 16-byte
+// aligned) one row per thread.
+template <class F4, class F1>
+__device__ __forceinline__ void cg_rows4(int row0, int row1, bool vec, F4&& f4, F1&& f1) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int a0 = vec ? min(row1, (row0 + 3) & ~3) : row1;
+  const int a1 = vec ? max(a0, row1 & ~3) : row1;
+#pragma unroll 2
+  for (int i = a0 + 4 * tid; i < a1; i += 4 * nt) f4(i);
+  for (int i = row0 + tid; i < a0; i += nt) f1(i);
+  for (int i = a1 + tid; i < row1; i += nt) f1(i);
+}
+__device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
+  const float4 t = *reinterpret_cast<const float4*>(p);
+  v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double (&v)[4]) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void st4(float* p, const float (&v)[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st4(double* p, const double (&v)[4]) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
+__device__ __forceinline__ bool aligned16(const void* a) { return (reinterpret_cast<uintptr_t>(a) & 15) == 0; }
+
 // Plain CG in one precision T (double, or float with the reference's float
 // build rounding of the scalars r.r, p.Ap, alpha and beta).
 template <class T>
@@ -243,6 +274,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
   GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G)}};
   const int tid = threadIdx.x, nt = blockDim.x;
+  const bool xvec = aligned16(x);  // the caller's solution vector
 
   // r = b - A x ; rr = r.r ; bb = b.b  (per-thread sums in T, then double)
   T rr_t = T(0), bb_t = T(0);
@@ -293,9 +325,20 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
     } else {
       if (k > 1) {
         const T beta = r1 / r0;
-        CG_ROWS(i, { p[i] = fma(beta, p[i], r[i]); })
+        cg_rows4(row0, row1, true, [&](int i) {
+          T pv[4], rv[4];
+          ld4(p + i, pv);
+          ld4(r + i, rv);
+#pragma unroll
+          for (int u = 0; u < 4; u++) pv[u] = fma(beta, pv[u], rv[u]);
+          st4(p + i, pv);
+        }, [&](int i) { p[i] = fma(beta, p[i], r[i]); });
       } else {
-        CG_ROWS(i, { p[i] = r[i]; })
+        cg_rows4(row0, row1, true, [&](int i) {
+          T rv[4];
+          ld4(r + i, rv);
+          st4(p + i, rv);
+        }, [&](int i) { p[i] = r[i]; });
       }
       if (!gs.gb.sync()) return;
       CG_ROWS(i, {
@@ -313,12 +356,26 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
     }
     const T alpha = r1 / dot;
     T rrn_t = T(0);
-    CG_ROWS(i, {
+    cg_rows4(row0, row1, xvec, [&](int i) {
+      T xv[4], pv[4], av[4], rv[4];
+      ld4(x + i, xv);
+      ld4(p + i, pv);
+      ld4(Ap + i, av);
+      ld4(r + i, rv);
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        xv[u] = fma(alpha, pv[u], xv[u]);
+        rv[u] = fma(-alpha, av[u], rv[u]);
+        rrn_t = fma(rv[u], rv[u], rrn_t);
+      }
+      st4(x + i, xv);
+      st4(r + i, rv);
+    }, [&](int i) {
       x[i] = fma(alpha, p[i], x[i]);
       const T ri = fma(-alpha, Ap[i], r[i]);
       r[i] = ri;
       rrn_t = fma(ri, ri, rrn_t);
-    })
+    });
     double rrn = double(rrn_t);
     if (!gs.sum1(3, rrn)) return;
     r0 = r1;
@@ -407,12 +464,26 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
     }
     const float alpha = float(rr / pap);
     float rrn_t = 0.0f;
-    CG_ROWS(i, {
+    cg_rows4(row0, row1, true, [&](int i) {
+      float xv[4], pv[4], av[4], rv[4];
+      ld4(xs + i, xv);
+      ld4(p + i, pv);
+      ld4(Ap + i, av);
+      ld4(r + i, rv);
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        xv[u] = fmaf(alpha, pv[u], xv[u]);
+        rv[u] = fmaf(-alpha, av[u], rv[u]);
+        rrn_t = fmaf(rv[u], rv[u], rrn_t);
+      }
+      st4(xs + i, xv);
+      st4(r + i, rv);
+    }, [&](int i) {
       xs[i] = fmaf(alpha, p[i], xs[i]);
       const float ri = fmaf(-alpha, Ap[i], r[i]);
       r[i] = ri;
       rrn_t = fmaf(ri, ri, rrn_t);
-    })
+    });
     double rrn = double(rrn_t);
     if (!gs.sum1(3, rrn)) return;
     since++;
