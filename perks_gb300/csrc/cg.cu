@@ -242,6 +242,21 @@ __device__ __forceinline__ void cg_rows4(int row0, int row1, bool vec, F4&& f4, 
   for (int i = row0 + tid; i < a0; i += nt) f1(i);
   for (int i = a1 + tid; i < row1; i += nt) f1(i);
 }
+// Row-strided loop (rows i, i+nt, ...: a warp's rows are consecutive, so CSR
+// row pointers and the rows' entries stay close together), kU rows per pass.
+template <class F1>
+__device__ __forceinline__ void cg_rows1(int row0, int row1, F1&& f1) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  CG_ROWS(i, { f1(i); })
+}
+// SpMV phase rows: DIA in groups of four rows, CSR row-strided.
+template <class F4, class F1>
+__device__ __forceinline__ void cg_rows_spmv(const CgMat& A, int row0, int row1, F4&& f4, F1&& f1) {
+  if (A.fmt == 1)
+    cg_rows4(row0, row1, true, f4, f1);
+  else
+    cg_rows1(row0, row1, f1);
+}
 __device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
   const float4 t = *reinterpret_cast<const float4*>(p);
   v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
@@ -259,6 +274,37 @@ __device__ __forceinline__ void st4(double* p, const double (&v)[4]) {
 }
 __device__ __forceinline__ bool aligned16(const void* a) { return (reinterpret_cast<uintptr_t>(a) & 15) == 0; }
 
+// Rows i..i+3 of A times the vector xv(column), each row in the same order as
+// spmv_row_f. DIA runs diagonal-major over the four rows: one 16-byte load of
+// the diagonal's values (when every diagonal starts 16-byte aligned) and four
+// independent gathers per diagonal, so a thread keeps many loads in flight.
+template <class XV, class MV, class XF>
+__device__ __forceinline__ void spmv4(const CgMat& A, const MV* __restrict__ val, bool v4, const XF& xv, int i,
+                                      XV (&acc)[4]) {
+  if (A.fmt == 0) {
+#pragma unroll
+    for (int u = 0; u < 4; u++) acc[u] = spmv_row_f<XV>(A, val, xv, i + u);
+  } else {
+#pragma unroll
+    for (int u = 0; u < 4; u++) acc[u] = XV(0);
+#pragma unroll 2
+    for (int k = 0; k < A.ndiag; k++) {
+      const MV* vk = val + (size_t)k * A.n + i;
+      MV a[4];
+      if (v4) {
+        ld4(vk, a);
+      } else {
+#pragma unroll
+        for (int u = 0; u < 4; u++) a[u] = vk[u];
+      }
+      const int c = i + A.off[k];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (c + u >= 0 && c + u < A.n) acc[u] = fma(XV(a[u]), xv(c + u), acc[u]);
+    }
+  }
+}
+
 // Plain CG in one precision T (double, or float with the reference's float
 // build rounding of the scalars r.r, p.Ap, alpha and beta).
 template <class T>
@@ -275,6 +321,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
   GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G)}};
   const int tid = threadIdx.x, nt = blockDim.x;
   const bool xvec = aligned16(x);  // the caller's solution vector
+  const bool v4 = A.fmt == 1 && (A.n & 3) == 0 && aligned16(val);  // DIA diagonals 16-byte aligned
 
   // r = b - A x ; rr = r.r ; bb = b.b  (per-thread sums in T, then double)
   T rr_t = T(0), bb_t = T(0);
@@ -306,21 +353,43 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
       if (k > 1) {
         const T beta = r1 / r0;
         const T* __restrict__ po = static_cast<const T*>(P.p[(k + 1) & 1]);
-        CG_ROWS(i, {
-          const T api = spmv_row_f<T>(A, val, [&](int c) { return fma(beta, po[c], r[c]); }, i);
+        auto pg = [&](int c) { return fma(beta, po[c], r[c]); };
+        cg_rows_spmv(A, row0, row1, [&](int i) {
+          T av[4], pov[4], rv[4], pv[4];
+          spmv4<T>(A, val, v4, pg, i, av);
+          ld4(po + i, pov);
+          ld4(r + i, rv);
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            pv[u] = fma(beta, pov[u], rv[u]);
+            pap_t = fma(pv[u], av[u], pap_t);
+          }
+          st4(p + i, pv);
+          st4(Ap + i, av);
+        }, [&](int i) {
+          const T api = spmv_row_f<T>(A, val, pg, i);
           const T pi = fma(beta, po[i], r[i]);
           p[i] = pi;
           Ap[i] = api;
           pap_t = fma(pi, api, pap_t);
-        })
+        });
       } else {
-        CG_ROWS(i, {
-          const T api = spmv_row(A, val, static_cast<const T*>(r), i);
+        auto rg = [&](int c) { return r[c]; };
+        cg_rows_spmv(A, row0, row1, [&](int i) {
+          T av[4], rv[4];
+          spmv4<T>(A, val, v4, rg, i, av);
+          ld4(r + i, rv);
+#pragma unroll
+          for (int u = 0; u < 4; u++) pap_t = fma(rv[u], av[u], pap_t);
+          st4(p + i, rv);
+          st4(Ap + i, av);
+        }, [&](int i) {
+          const T api = spmv_row_f<T>(A, val, rg, i);
           const T pi = r[i];
           p[i] = pi;
           Ap[i] = api;
           pap_t = fma(pi, api, pap_t);
-        })
+        });
       }
     } else {
       if (k > 1) {
@@ -341,11 +410,19 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
         }, [&](int i) { p[i] = r[i]; });
       }
       if (!gs.gb.sync()) return;
-      CG_ROWS(i, {
-        const T api = spmv_row(A, val, static_cast<const T*>(p), i);
+      auto pg = [&](int c) { return p[c]; };
+      cg_rows_spmv(A, row0, row1, [&](int i) {
+        T av[4], pv[4];
+        spmv4<T>(A, val, v4, pg, i, av);
+        ld4(p + i, pv);
+#pragma unroll
+        for (int u = 0; u < 4; u++) pap_t = fma(pv[u], av[u], pap_t);
+        st4(Ap + i, av);
+      }, [&](int i) {
+        const T api = spmv_row_f<T>(A, val, pg, i);
         Ap[i] = api;
         pap_t = fma(p[i], api, pap_t);
-      })
+      });
     }
     double pap = double(pap_t);
     if (!gs.sum1(1 + (k & 1), pap)) return;
@@ -405,6 +482,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
   GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G)}};
   const int tid = threadIdx.x, nt = blockDim.x;
+  const bool v4 = A.fmt == 1 && (A.n & 3) == 0;  // val32 (workspace) diagonals 16-byte aligned
 
   // FP32 copy of this CTA's matrix values (CSR nonzeros of its rows, or its
   // rows of every diagonal).
@@ -440,21 +518,43 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
     if (k > 1) {
       const float beta = float(rr / rr0);
       const float* __restrict__ po = static_cast<const float*>(P.p[(k + 1) & 1]);
-      CG_ROWS(i, {
-        const float api = spmv_row_f<float>(A, val32, [&](int c) { return fmaf(beta, po[c], r[c]); }, i);
+      auto pg = [&](int c) { return fmaf(beta, po[c], r[c]); };
+      cg_rows_spmv(A, row0, row1, [&](int i) {
+        float av[4], pov[4], rv[4], pv[4];
+        spmv4<float>(A, val32, v4, pg, i, av);
+        ld4(po + i, pov);
+        ld4(r + i, rv);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          pv[u] = fmaf(beta, pov[u], rv[u]);
+          pap_t = fmaf(pv[u], av[u], pap_t);
+        }
+        st4(p + i, pv);
+        st4(Ap + i, av);
+      }, [&](int i) {
+        const float api = spmv_row_f<float>(A, val32, pg, i);
         const float pi = fmaf(beta, po[i], r[i]);
         p[i] = pi;
         Ap[i] = api;
         pap_t = fmaf(pi, api, pap_t);
-      })
+      });
     } else {
-      CG_ROWS(i, {
-        const float api = spmv_row(A, val32, static_cast<const float*>(r), i);
+      auto rg = [&](int c) { return r[c]; };
+      cg_rows_spmv(A, row0, row1, [&](int i) {
+        float av[4], rv[4];
+        spmv4<float>(A, val32, v4, rg, i, av);
+        ld4(r + i, rv);
+#pragma unroll
+        for (int u = 0; u < 4; u++) pap_t = fmaf(rv[u], av[u], pap_t);
+        st4(p + i, rv);
+        st4(Ap + i, av);
+      }, [&](int i) {
+        const float api = spmv_row_f<float>(A, val32, rg, i);
         const float pi = r[i];
         p[i] = pi;
         Ap[i] = api;
         pap_t = fmaf(pi, api, pap_t);
-      })
+      });
     }
     double pap = double(pap_t);
     if (!gs.sum1(1 + (k & 1), pap)) return;
