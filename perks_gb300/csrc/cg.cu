@@ -17,8 +17,15 @@
 // every CTA adds all partials in the same fixed order, so all CTAs derive
 // identical alpha / beta without atomics.
 //
-// Rows are split between CTAs by a merge-path split of rows + nonzeros, so
-// irregular CSR rows are balanced; within a CTA a thread owns a row.
+// CSR rows are split between CTAs by a merge-path split of rows + nonzeros,
+// so irregular rows are balanced. A CSR matrix whose longest row has at most
+// 64 entries and whose rows are near that length (ELL padding <= 25%, e.g.
+// the Laplacians) is copied at the start of the solve into a column-major ELL
+// layout (entry k of row i at k*n + i, short rows padded with column i and
+// value 0): the SpMV then reads it coalesced, four rows per thread, in the
+// CSR entry order. The running sum is never -0 (it starts at +0 and exact
+// cancellation rounds to +0), so a padding term fma(0, x_i, acc) leaves it
+// unchanged and the results equal the CSR ones for finite values.
 //
 // Mixed precision (reliable updates, Sleijpen & van der Vorst 1996): the
 // Krylov iteration runs in FP32 (FP32 copy of the matrix values and FP32
@@ -41,23 +48,26 @@ constexpr int kCgThreads = 1024;
 constexpr int kMaxDiag = 32;
 
 struct CgMat {
-  int n, nnz, fmt;        // fmt 0 = CSR, 1 = DIA
+  int n, nnz, fmt;        // fmt 0 = CSR, 1 = DIA, 2 = ELL (column-major, ew entries per row)
   const int* rp;          // CSR
   const int* ci;
   const void* val;        // CSR values or DIA data (dtype of the solve, FP64 for mixed)
   int ndiag;
   int off[kMaxDiag];
+  const int* eci;         // ELL column indices [ew][n]
+  int ew;
 };
 
 struct CgParams {
-  CgMat A;
+  CgMat A;                // the working-precision SpMV (may be the ELL copy)
+  CgMat A64;              // mixed precision: the FP64 matrix as given (true residual)
   const void* b;
   void* x;                // in: x0, out: solution (FP64 for FP64/mixed, FP32 for FP32)
   void* r;                // working vectors, working precision
   void* p[2];             // p; FP32 and mixed alternate the two buffers between iterations
   void* Ap;
   // mixed precision extras
-  float* val32;           // FP32 copy of the matrix values (CSR nnz or DIA ndiag*n)
+  float* val32;           // FP32 copy of the matrix values, in A's layout (built before the launch)
   double* r64;            // FP64 true residual
   float* xs;              // FP32 solution increment
   double* part;           // [4][gridDim] partial sums
@@ -86,10 +96,12 @@ __device__ __forceinline__ int cg_split(const CgMat& A, int c, int ncta) {
 
 // Row i of A times a vector given by xv(column). Accumulates in the working
 // precision XV (double for FP64, float for FP32).
-template <class XV, class MV, class XF>
+// FMT >= 0 fixes the format at compile time (the other paths drop out).
+template <class XV, int FMT = -1, class MV, class XF>
 __device__ __forceinline__ XV spmv_row_f(const CgMat& A, const MV* __restrict__ val, const XF& xv, int i) {
+  const int fmt = FMT >= 0 ? FMT : A.fmt;
   XV acc = XV(0);
-  if (A.fmt == 0) {
+  if (fmt == 0) {
     const int j0 = __ldg(A.rp + i), j1 = __ldg(A.rp + i + 1);
     int j = j0;
     // four independent gathers in flight per row
@@ -103,6 +115,11 @@ __device__ __forceinline__ XV spmv_row_f(const CgMat& A, const MV* __restrict__ 
       acc = fma(v3, x3, acc);
     }
     for (; j < j1; j++) acc = fma(XV(__ldg(val + j)), xv(__ldg(A.ci + j)), acc);
+  } else if (fmt == 2) {
+    for (int k = 0; k < A.ew; k++) {
+      const size_t e = (size_t)k * A.n + i;
+      acc = fma(XV(__ldg(val + e)), xv(__ldg(A.eci + e)), acc);
+    }
   } else {
 #pragma unroll 8
     for (int k = 0; k < A.ndiag; k++) {
@@ -113,9 +130,9 @@ __device__ __forceinline__ XV spmv_row_f(const CgMat& A, const MV* __restrict__ 
   }
   return acc;
 }
-template <class MV, class XV>
+template <int FMT = -1, class MV, class XV>
 __device__ __forceinline__ XV spmv_row(const CgMat& A, const MV* __restrict__ val, const XV* __restrict__ x, int i) {
-  return spmv_row_f<XV>(A, val, [x](int c) { return x[c]; }, i);
+  return spmv_row_f<XV, FMT>(A, val, [x](int c) { return x[c]; }, i);
 }
 
 // Block-wide sum of two doubles; result valid in every thread.
@@ -249,10 +266,10 @@ __device__ __forceinline__ void cg_rows1(int row0, int row1, F1&& f1) {
   const int tid = threadIdx.x, nt = blockDim.x;
   CG_ROWS(i, { f1(i); })
 }
-// SpMV phase rows: DIA in groups of four rows, CSR row-strided.
-template <class F4, class F1>
+// SpMV phase rows: DIA and ELL in groups of four rows, CSR row-strided.
+template <int FMT, class F4, class F1>
 __device__ __forceinline__ void cg_rows_spmv(const CgMat& A, int row0, int row1, F4&& f4, F1&& f1) {
-  if (A.fmt == 1)
+  if ((FMT >= 0 ? FMT : A.fmt) != 0)
     cg_rows4(row0, row1, true, f4, f1);
   else
     cg_rows1(row0, row1, f1);
@@ -278,12 +295,35 @@ __device__ __forceinline__ bool aligned16(const void* a) { return (reinterpret_c
 // spmv_row_f. DIA runs diagonal-major over the four rows: one 16-byte load of
 // the diagonal's values (when every diagonal starts 16-byte aligned) and four
 // independent gathers per diagonal, so a thread keeps many loads in flight.
-template <class XV, class MV, class XF>
+template <class XV, int FMT = -1, class MV, class XF>
 __device__ __forceinline__ void spmv4(const CgMat& A, const MV* __restrict__ val, bool v4, const XF& xv, int i,
                                       XV (&acc)[4]) {
-  if (A.fmt == 0) {
+  const int fmt = FMT >= 0 ? FMT : A.fmt;
+  if (fmt == 0) {
 #pragma unroll
-    for (int u = 0; u < 4; u++) acc[u] = spmv_row_f<XV>(A, val, xv, i + u);
+    for (int u = 0; u < 4; u++) acc[u] = spmv_row_f<XV, FMT>(A, val, xv, i + u);
+  } else if (fmt == 2) {
+#pragma unroll
+    for (int u = 0; u < 4; u++) acc[u] = XV(0);
+#pragma unroll 2
+    for (int k = 0; k < A.ew; k++) {
+      const size_t e = (size_t)k * A.n + i;
+      MV a[4];
+      int c[4];
+      if (v4) {
+        ld4(val + e, a);
+        const int4 t = *reinterpret_cast<const int4*>(A.eci + e);
+        c[0] = t.x; c[1] = t.y; c[2] = t.z; c[3] = t.w;
+      } else {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          a[u] = val[e + u];
+          c[u] = A.eci[e + u];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) acc[u] = fma(XV(a[u]), xv(c[u]), acc[u]);
+    }
   } else {
 #pragma unroll
     for (int u = 0; u < 4; u++) acc[u] = XV(0);
@@ -307,7 +347,7 @@ __device__ __forceinline__ void spmv4(const CgMat& A, const MV* __restrict__ val
 
 // Plain CG in one precision T (double, or float with the reference's float
 // build rounding of the scalars r.r, p.Ap, alpha and beta).
-template <class T>
+template <class T, int FMT>
 __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_constant__ CgParams P) {
   constexpr bool FUSE = sizeof(T) == 4;  // p formed in the SpMV gather
   const CgMat& A = P.A;
@@ -321,12 +361,12 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
   GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G)}};
   const int tid = threadIdx.x, nt = blockDim.x;
   const bool xvec = aligned16(x);  // the caller's solution vector
-  const bool v4 = A.fmt == 1 && (A.n & 3) == 0 && aligned16(val);  // DIA diagonals 16-byte aligned
+  const bool v4 = A.fmt != 0 && (A.n & 3) == 0 && aligned16(val) && aligned16(A.eci);  // DIA/ELL columns 16-byte aligned
 
   // r = b - A x ; rr = r.r ; bb = b.b  (per-thread sums in T, then double)
   T rr_t = T(0), bb_t = T(0);
   CG_ROWS(i, {
-    const T ax = spmv_row(A, val, x, i);
+    const T ax = spmv_row<FMT>(A, val, x, i);
     const T bi = b[i];
     const T ri = T(-1) * ax + bi;
     r[i] = ri;
@@ -354,9 +394,9 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
         const T beta = r1 / r0;
         const T* __restrict__ po = static_cast<const T*>(P.p[(k + 1) & 1]);
         auto pg = [&](int c) { return fma(beta, po[c], r[c]); };
-        cg_rows_spmv(A, row0, row1, [&](int i) {
+        cg_rows_spmv<FMT>(A, row0, row1, [&](int i) {
           T av[4], pov[4], rv[4], pv[4];
-          spmv4<T>(A, val, v4, pg, i, av);
+          spmv4<T, FMT>(A, val, v4, pg, i, av);
           ld4(po + i, pov);
           ld4(r + i, rv);
 #pragma unroll
@@ -367,7 +407,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
           st4(p + i, pv);
           st4(Ap + i, av);
         }, [&](int i) {
-          const T api = spmv_row_f<T>(A, val, pg, i);
+          const T api = spmv_row_f<T, FMT>(A, val, pg, i);
           const T pi = fma(beta, po[i], r[i]);
           p[i] = pi;
           Ap[i] = api;
@@ -375,16 +415,16 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
         });
       } else {
         auto rg = [&](int c) { return r[c]; };
-        cg_rows_spmv(A, row0, row1, [&](int i) {
+        cg_rows_spmv<FMT>(A, row0, row1, [&](int i) {
           T av[4], rv[4];
-          spmv4<T>(A, val, v4, rg, i, av);
+          spmv4<T, FMT>(A, val, v4, rg, i, av);
           ld4(r + i, rv);
 #pragma unroll
           for (int u = 0; u < 4; u++) pap_t = fma(rv[u], av[u], pap_t);
           st4(p + i, rv);
           st4(Ap + i, av);
         }, [&](int i) {
-          const T api = spmv_row_f<T>(A, val, rg, i);
+          const T api = spmv_row_f<T, FMT>(A, val, rg, i);
           const T pi = r[i];
           p[i] = pi;
           Ap[i] = api;
@@ -411,15 +451,15 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
       }
       if (!gs.gb.sync()) return;
       auto pg = [&](int c) { return p[c]; };
-      cg_rows_spmv(A, row0, row1, [&](int i) {
+      cg_rows_spmv<FMT>(A, row0, row1, [&](int i) {
         T av[4], pv[4];
-        spmv4<T>(A, val, v4, pg, i, av);
+        spmv4<T, FMT>(A, val, v4, pg, i, av);
         ld4(p + i, pv);
 #pragma unroll
         for (int u = 0; u < 4; u++) pap_t = fma(pv[u], av[u], pap_t);
         st4(Ap + i, av);
       }, [&](int i) {
-        const T api = spmv_row_f<T>(A, val, pg, i);
+        const T api = spmv_row_f<T, FMT>(A, val, pg, i);
         Ap[i] = api;
         pap_t = fma(p[i], api, pap_t);
       });
@@ -468,9 +508,12 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
 
 // ---------------------------------------------------------------------------
 // Mixed precision: FP32 Krylov iteration, FP64 solution and true residual.
+template <int FMT>
 __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant__ CgParams P) {
-  const CgMat& A = P.A;
-  const double* __restrict__ val64 = static_cast<const double*>(A.val);
+  constexpr int FMT64 = FMT == 2 ? 0 : FMT;  // the FP64 matrix is the given CSR or DIA
+  const CgMat& A = P.A;      // FP32 iteration (values in val32)
+  const CgMat& A64 = P.A64;  // FP64 true residual
+  const double* __restrict__ val64 = static_cast<const double*>(A64.val);
   float* __restrict__ val32 = P.val32;
   const double* __restrict__ b = static_cast<const double*>(P.b);
   double* __restrict__ x = static_cast<double*>(P.x);
@@ -482,22 +525,13 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
   GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G)}};
   const int tid = threadIdx.x, nt = blockDim.x;
-  const bool v4 = A.fmt == 1 && (A.n & 3) == 0;  // val32 (workspace) diagonals 16-byte aligned
+  const bool v4 = A.fmt != 0 && (A.n & 3) == 0 && aligned16(A.eci);  // val32 (workspace) is aligned
 
-  // FP32 copy of this CTA's matrix values (CSR nonzeros of its rows, or its
-  // rows of every diagonal).
-  if (A.fmt == 0) {
-    const int j0 = A.rp[row0], j1 = A.rp[row1];
-    for (int j = j0 + tid; j < j1; j += nt) val32[j] = float(val64[j]);
-  } else {
-    for (int kd = 0; kd < A.ndiag; kd++)
-      for (int i = row0 + tid; i < row1; i += nt) val32[(size_t)kd * A.n + i] = float(val64[(size_t)kd * A.n + i]);
-  }
-  // true residual in FP64
+  // true residual in FP64 (rows split as for A: A64 has the same rows)
   double rr = 0.0, bb = 0.0;
   CG_ROWS(i, {
     const double bi = b[i];
-    const double ri = bi - spmv_row(A, val64, x, i);
+    const double ri = bi - spmv_row<FMT64>(A64, val64, x, i);
     r64[i] = ri;
     r[i] = float(ri);
     xs[i] = 0.0f;
@@ -519,9 +553,9 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       const float beta = float(rr / rr0);
       const float* __restrict__ po = static_cast<const float*>(P.p[(k + 1) & 1]);
       auto pg = [&](int c) { return fmaf(beta, po[c], r[c]); };
-      cg_rows_spmv(A, row0, row1, [&](int i) {
+      cg_rows_spmv<FMT>(A, row0, row1, [&](int i) {
         float av[4], pov[4], rv[4], pv[4];
-        spmv4<float>(A, val32, v4, pg, i, av);
+        spmv4<float, FMT>(A, val32, v4, pg, i, av);
         ld4(po + i, pov);
         ld4(r + i, rv);
 #pragma unroll
@@ -532,7 +566,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
         st4(p + i, pv);
         st4(Ap + i, av);
       }, [&](int i) {
-        const float api = spmv_row_f<float>(A, val32, pg, i);
+        const float api = spmv_row_f<float, FMT>(A, val32, pg, i);
         const float pi = fmaf(beta, po[i], r[i]);
         p[i] = pi;
         Ap[i] = api;
@@ -540,16 +574,16 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       });
     } else {
       auto rg = [&](int c) { return r[c]; };
-      cg_rows_spmv(A, row0, row1, [&](int i) {
+      cg_rows_spmv<FMT>(A, row0, row1, [&](int i) {
         float av[4], rv[4];
-        spmv4<float>(A, val32, v4, rg, i, av);
+        spmv4<float, FMT>(A, val32, v4, rg, i, av);
         ld4(r + i, rv);
 #pragma unroll
         for (int u = 0; u < 4; u++) pap_t = fmaf(rv[u], av[u], pap_t);
         st4(p + i, rv);
         st4(Ap + i, av);
       }, [&](int i) {
-        const float api = spmv_row_f<float>(A, val32, rg, i);
+        const float api = spmv_row_f<float, FMT>(A, val32, rg, i);
         const float pi = r[i];
         p[i] = pi;
         Ap[i] = api;
@@ -598,7 +632,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       if (!gs.gb.sync()) return;
       double rt = 0.0;
       CG_ROWS(i, {
-        const double ri = b[i] - spmv_row(A, val64, x, i);
+        const double ri = b[i] - spmv_row<FMT64>(A64, val64, x, i);
         r64[i] = ri;
         r[i] = float(ri);
         rt = fma(ri, ri, rt);
@@ -778,6 +812,31 @@ __global__ void spmv_kernel(CgMat A, const T* x, T* y) {
     y[i] = T(spmv_row(A, val, x, i));
 }
 
+// Longest CSR row (setup for the ELL choice).
+__global__ void csr_max_row(const int* rp, int n, int* out) {
+  int m = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) m = max(m, rp[i + 1] - rp[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+// CSR -> column-major ELL with ew entries per row, values converted to DV.
+template <class SV, class DV>
+__global__ void ell_build(const int* rp, const int* ci, const SV* val, int n, int ew, int* eci, DV* ev) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int j0 = rp[i], len = rp[i + 1] - j0;
+    for (int k = 0; k < ew; k++) {
+      const size_t e = (size_t)k * n + i;
+      eci[e] = k < len ? ci[j0 + k] : i;
+      ev[e] = k < len ? DV(val[j0 + k]) : DV(0);
+    }
+  }
+}
+__global__ void to_f32(const double* src, size_t n, float* dst) {
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+    dst[i] = float(src[i]);
+}
+
 // ---------------------------------------------------------------------------
 // Host side
 static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, perks_cg_result* res) {
@@ -838,15 +897,63 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   P.status = sw.status;
   PERKS_CUDA(cudaMemsetAsync(scal, 0, 32 * sizeof(double), s));
 
+  // The timed region includes the matrix setup below.
   cudaEvent_t e0, e1;
   PERKS_CUDA(cudaEventCreate(&e0));
   PERKS_CUDA(cudaEventCreate(&e1));
   PERKS_CUDA(cudaEventRecord(e0, s));
+
+  // Working matrix of the persistent kernels: CSR with bounded rows -> ELL.
+  P.A64 = A;
+  const bool mixed = o->dtype == PERKS_MIXED;
+  if (A.fmt == 0 && o->kernel == PERKS_KERNEL_PERSISTENT && n > 0) {
+    int* mx = reinterpret_cast<int*>(scal + 24);
+    csr_max_row<<<dev->sms * 4, 256, 0, s>>>(A.rp, n, mx);
+    int ew = 0;
+    PERKS_CUDA(cudaMemcpyAsync(&ew, mx, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PERKS_CUDA(cudaStreamSynchronize(s));
+    count_launch(1);
+    if (ew >= 1 && ew <= 64 && 4ll * ew * n <= 5ll * std::max(A.nnz, 1)) {
+      const size_t evb = (f32 || mixed) ? 4 : 8;
+      const size_t ci_bytes = (size_t(ew) * n * 4 + 255) & ~size_t(255);
+      unsigned char* m = static_cast<unsigned char*>(workspace(kWsCgMat, ci_bytes + size_t(ew) * n * evb, &st));
+      if (!m) return st;
+      int* eci = reinterpret_cast<int*>(m);
+      void* ev = m + ci_bytes;
+      const int g = dev->sms * 8;
+      if (f32)
+        ell_build<float, float><<<g, 256, 0, s>>>(A.rp, A.ci, static_cast<const float*>(A.val), n, ew, eci,
+                                                   static_cast<float*>(ev));
+      else if (mixed)
+        ell_build<double, float><<<g, 256, 0, s>>>(A.rp, A.ci, static_cast<const double*>(A.val), n, ew, eci,
+                                                    static_cast<float*>(ev));
+      else
+        ell_build<double, double><<<g, 256, 0, s>>>(A.rp, A.ci, static_cast<const double*>(A.val), n, ew, eci,
+                                                     static_cast<double*>(ev));
+      PERKS_CUDA(cudaGetLastError());
+      count_launch(1);
+      P.A.fmt = 2;
+      P.A.ew = ew;
+      P.A.eci = eci;
+      P.A.val = mixed ? nullptr : ev;
+      if (mixed) P.val32 = static_cast<float*>(ev);
+    }
+  }
+  if (mixed && P.A.fmt != 2) {
+    to_f32<<<dev->sms * 8, 256, 0, s>>>(static_cast<const double*>(A.val), nval, P.val32);
+    PERKS_CUDA(cudaGetLastError());
+    count_launch(1);
+  }
+
   int launches = 0;
   if (o->kernel == PERKS_KERNEL_PERSISTENT) {
-    const void* kern = o->dtype == PERKS_MIXED ? (const void*)cg_mixed
-                       : f32                   ? (const void*)cg_persistent<float>
-                                               : (const void*)cg_persistent<double>;
+    const int f = P.A.fmt;
+    const void* kern =
+        o->dtype == PERKS_MIXED ? (f == 0 ? (const void*)cg_mixed<0> : f == 1 ? (const void*)cg_mixed<1> : (const void*)cg_mixed<2>)
+        : f32 ? (f == 0 ? (const void*)cg_persistent<float, 0> : f == 1 ? (const void*)cg_persistent<float, 1>
+                                                                 : (const void*)cg_persistent<float, 2>)
+              : (f == 0 ? (const void*)cg_persistent<double, 0> : f == 1 ? (const void*)cg_persistent<double, 1>
+                                                                  : (const void*)cg_persistent<double, 2>);
     int per_sm = 0;
     PERKS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCgThreads, 0));
     if (per_sm < 1) return fail(PERKS_ERR_LAUNCH, "CG kernel does not fit on an SM");
