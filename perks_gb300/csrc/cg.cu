@@ -18,7 +18,10 @@
 // identical alpha / beta without atomics.
 //
 // CSR rows are split between CTAs by a merge-path split of rows + nonzeros,
-// so irregular rows are balanced. A CSR matrix whose longest row has at most
+// so irregular rows are balanced. A CSR matrix with sorted, unique columns
+// whose entries lie on at most 32 diagonals (DIA padding <= 25%) is copied at
+// the start of the solve into the DIA layout (diagonals ascending = columns
+// ascending, the CSR entry order). Otherwise, a CSR matrix whose longest row has at most
 // 64 entries and whose rows are near that length (ELL padding <= 25%, e.g.
 // the Laplacians) is copied at the start of the solve into a column-major ELL
 // layout (entry k of row i at k*n + i, short rows padded with column i and
@@ -39,6 +42,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <vector>
 #include "ptx.cuh"
 #include "runtime.cuh"
 
@@ -508,9 +512,8 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
 
 // ---------------------------------------------------------------------------
 // Mixed precision: FP32 Krylov iteration, FP64 solution and true residual.
-template <int FMT>
+template <int FMT, int FMT64>  // FMT64: the format of the FP64 matrix as given (CSR or DIA)
 __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant__ CgParams P) {
-  constexpr int FMT64 = FMT == 2 ? 0 : FMT;  // the FP64 matrix is the given CSR or DIA
   const CgMat& A = P.A;      // FP32 iteration (values in val32)
   const CgMat& A64 = P.A64;  // FP64 true residual
   const double* __restrict__ val64 = static_cast<const double*>(A64.val);
@@ -832,6 +835,44 @@ __global__ void ell_build(const int* rp, const int* ci, const SV* val, int n, in
     }
   }
 }
+// Distinct diagonal offsets of a CSR matrix into a 64-slot open-addressing
+// table (kEmpty = unused); flags[0]: more than 64 distinct, flags[1]: a row
+// whose columns are not strictly increasing.
+constexpr int kEmpty = 0x7fffffff;
+__global__ void csr_diag_scan(const int* rp, const int* ci, int n, int* tab, int* flags) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int j0 = rp[i], j1 = rp[i + 1];
+    int prev = -1;
+    for (int j = j0; j < j1; j++) {
+      const int c = ci[j];
+      if (c <= prev) flags[1] = 1;
+      prev = c;
+      const int d = c - i;
+      int h = (d * 40503) & 63, probes = 0;
+      for (; probes < 64; probes++, h = (h + 1) & 63) {
+        const int t = *((volatile int*)(tab + h));
+        if (t == d) break;
+        if (t == kEmpty) {
+          const int old = atomicCAS(tab + h, kEmpty, d);
+          if (old == kEmpty || old == d) break;
+        }
+      }
+      if (probes == 64) flags[0] = 1;
+    }
+  }
+}
+// CSR -> DIA (data zeroed beforehand), values converted to DV.
+template <class SV, class DV>
+__global__ void dia_build(CgMat D, const int* rp, const int* ci, const SV* val, DV* data) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.n; i += gridDim.x * blockDim.x) {
+    int k = 0;
+    for (int j = rp[i]; j < rp[i + 1]; j++) {
+      const int d = ci[j] - i;
+      while (k < D.ndiag - 1 && D.off[k] != d) k++;  // columns ascend, so diagonals do too
+      data[(size_t)k * D.n + i] = DV(val[j]);
+    }
+  }
+}
 __global__ void to_f32(const double* src, size_t n, float* dst) {
   for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
     dst[i] = float(src[i]);
@@ -906,7 +947,51 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   // Working matrix of the persistent kernels: CSR with bounded rows -> ELL.
   P.A64 = A;
   const bool mixed = o->dtype == PERKS_MIXED;
+  bool as_dia = false;
   if (A.fmt == 0 && o->kernel == PERKS_KERNEL_PERSISTENT && n > 0) {
+    // 64 table slots + 2 flags in the CG vector workspace's spare tail
+    int* tab = reinterpret_cast<int*>(scal + 32);
+    int* flags = tab + 64;
+    std::vector<int> init(66, kEmpty);
+    init[64] = init[65] = 0;
+    PERKS_CUDA(cudaMemcpyAsync(tab, init.data(), 66 * sizeof(int), cudaMemcpyHostToDevice, s));
+    csr_diag_scan<<<dev->sms * 8, 256, 0, s>>>(A.rp, A.ci, n, tab, flags);
+    std::vector<int> got(66);
+    PERKS_CUDA(cudaMemcpyAsync(got.data(), tab, 66 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    PERKS_CUDA(cudaStreamSynchronize(s));
+    count_launch(1);
+    std::vector<int> offs;
+    for (int h = 0; h < 64; h++)
+      if (got[h] != kEmpty) offs.push_back(got[h]);
+    std::sort(offs.begin(), offs.end());
+    if (!got[64] && !got[65] && !offs.empty() && int(offs.size()) <= kMaxDiag &&
+        4ll * (long long)offs.size() * n <= 5ll * std::max(A.nnz, 1)) {
+      const size_t evb = (f32 || mixed) ? 4 : 8;
+      const size_t bytes = offs.size() * size_t(n) * evb;
+      void* data = workspace(kWsCgMat, bytes, &st);
+      if (!data) return st;
+      PERKS_CUDA(cudaMemsetAsync(data, 0, bytes, s));
+      CgMat D{};
+      D.n = n;
+      D.fmt = 1;
+      D.ndiag = int(offs.size());
+      for (int k = 0; k < D.ndiag; k++) D.off[k] = offs[k];
+      const int g = dev->sms * 8;
+      if (f32)
+        dia_build<float, float><<<g, 256, 0, s>>>(D, A.rp, A.ci, static_cast<const float*>(A.val), static_cast<float*>(data));
+      else if (mixed)
+        dia_build<double, float><<<g, 256, 0, s>>>(D, A.rp, A.ci, static_cast<const double*>(A.val), static_cast<float*>(data));
+      else
+        dia_build<double, double><<<g, 256, 0, s>>>(D, A.rp, A.ci, static_cast<const double*>(A.val), static_cast<double*>(data));
+      PERKS_CUDA(cudaGetLastError());
+      count_launch(1);
+      D.val = mixed ? nullptr : data;
+      P.A = D;
+      if (mixed) P.val32 = static_cast<float*>(data);
+      as_dia = true;
+    }
+  }
+  if (A.fmt == 0 && o->kernel == PERKS_KERNEL_PERSISTENT && n > 0 && !as_dia) {
     int* mx = reinterpret_cast<int*>(scal + 24);
     csr_max_row<<<dev->sms * 4, 256, 0, s>>>(A.rp, n, mx);
     int ew = 0;
@@ -939,7 +1024,7 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
       if (mixed) P.val32 = static_cast<float*>(ev);
     }
   }
-  if (mixed && P.A.fmt != 2) {
+  if (mixed && P.A.fmt == A.fmt) {  // no converted copy: FP32 copy of the given values
     to_f32<<<dev->sms * 8, 256, 0, s>>>(static_cast<const double*>(A.val), nval, P.val32);
     PERKS_CUDA(cudaGetLastError());
     count_launch(1);
@@ -949,7 +1034,10 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   if (o->kernel == PERKS_KERNEL_PERSISTENT) {
     const int f = P.A.fmt;
     const void* kern =
-        o->dtype == PERKS_MIXED ? (f == 0 ? (const void*)cg_mixed<0> : f == 1 ? (const void*)cg_mixed<1> : (const void*)cg_mixed<2>)
+        o->dtype == PERKS_MIXED
+            ? (f == 0 ? (const void*)cg_mixed<0, 0>
+               : f == 2 ? (const void*)cg_mixed<2, 0>
+               : A.fmt == 1 ? (const void*)cg_mixed<1, 1> : (const void*)cg_mixed<1, 0>)
         : f32 ? (f == 0 ? (const void*)cg_persistent<float, 0> : f == 1 ? (const void*)cg_persistent<float, 1>
                                                                  : (const void*)cg_persistent<float, 2>)
               : (f == 0 ? (const void*)cg_persistent<double, 0> : f == 1 ? (const void*)cg_persistent<double, 1>

@@ -117,3 +117,47 @@ def test_spmv_matches_oracle(native, cuda, oracle):
     x = np.random.default_rng(5).standard_normal(len(rp) - 1)
     y = native.spmv_dia(off, data, x, device=cuda).cpu().numpy()
     assert np.allclose(y, oracle.spmv_dia(off, data, x), rtol=1e-13, atol=1e-12)
+
+
+def _permuted(rp, ci, v, seed):
+    """P A P^T for a random permutation, columns sorted within rows."""
+    import scipy.sparse as sp
+    n = len(rp) - 1
+    A = sp.csr_matrix((v, ci, rp), shape=(n, n))
+    perm = np.random.default_rng(seed).permutation(n)
+    B = A[perm][:, perm].tocsr()
+    B.sort_indices()
+    return B.indptr.astype(np.int32), B.indices.astype(np.int32), B.data
+
+
+def _shuffled_columns(rp, ci, v, seed):
+    """The same matrix with each row's entries in a random order."""
+    rng = np.random.default_rng(seed)
+    ci2, v2 = ci.copy(), v.copy()
+    for i in range(len(rp) - 1):
+        a, b = rp[i], rp[i + 1]
+        o = rng.permutation(b - a) + a
+        ci2[a:b], v2[a:b] = ci[o], v[o]
+    return rp, ci2, v2
+
+
+# CSR layouts the persistent solver chooses internally: diagonal structure
+# (sorted columns, few diagonals: solved as DIA), bounded rows on scattered
+# diagonals (ELL copy), unsorted columns (ELL copy: the DIA copy needs sorted
+# columns), long irregular rows (CSR as given).
+@pytest.mark.parametrize("layout", ["diagonals", "scattered", "unsorted", "irregular"])
+@pytest.mark.parametrize("dtype", ["fp64", "mixed"])
+def test_cg_csr_layouts(native, cuda, oracle, layout, dtype):
+    pytest.importorskip("scipy")
+    from perks_gb300 import matrices as M
+    base = M.laplacian_2d(96)
+    rp, ci, v = {"diagonals": lambda: base, "scattered": lambda: _permuted(*base, seed=3),
+                 "unsorted": lambda: _shuffled_columns(*base, seed=4),
+                 "irregular": lambda: M.random_spd(20000, 5)}[layout]()
+    b = np.random.default_rng(6).uniform(-1, 1, len(rp) - 1)
+    _, it, _, _ = oracle.cg(rp, ci, v, b, max_iter=20000, stop=1, tol=1e-10)
+    x, res = native.cg_csr(rp, ci, v, b, dtype=dtype, tol=1e-10, device=cuda)
+    if dtype == "fp64":
+        assert it_close(res["iterations"], it), (layout, res, it)
+    assert res["true_rel_res"] <= 1e-10 * 1.05
+    assert true_rel(rp, ci, v, b, x.cpu().numpy()) <= 1e-10 * 1.05
