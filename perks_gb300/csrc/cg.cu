@@ -166,14 +166,17 @@ __device__ __forceinline__ void block_sum2(double& a, double& b) {
 
 // Block-wide sum of NV doubles, valid in thread 0 only: warps reduce by
 // shuffles, then warp 0 alone adds the warp sums (FP64 issue is scarce).
-template <int NV>
+// WARP_DONE: lane 0 of every warp already holds its warp's sum.
+template <int NV, bool WARP_DONE = false>
 __device__ __forceinline__ void block_sum_t0(double (&v)[NV]) {
   __shared__ double sw[NV][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if constexpr (!WARP_DONE) {
 #pragma unroll
-  for (int k = 0; k < NV; k++)
+    for (int k = 0; k < NV; k++)
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  }
   __syncthreads();  // the previous call's readers are done with sw
   if (lane == 0)
 #pragma unroll
@@ -195,9 +198,9 @@ __device__ __forceinline__ void block_sum_t0(double (&v)[NV]) {
 struct GridSum {
   double* part;  // [slot][2][gridDim]
   GridBarrier gb;
-  template <int NV>
+  template <int NV, bool WARP_DONE = false>
   __device__ bool sum(int slot, double (&v)[NV]) {
-    block_sum_t0<NV>(v);
+    block_sum_t0<NV, WARP_DONE>(v);
     const int G = gridDim.x;
     double* ps = part + size_t(slot) * 2 * G;
     if (threadIdx.x == 0)
@@ -233,6 +236,16 @@ struct GridSum {
     double v[1] = {a};
     if (!sum<1>(slot, v)) return false;
     a = v[0];
+    return true;
+  }
+  // An FP32 per-thread partial: summed across the warp in FP32 (FP64 issue
+  // is 1/64 of FP32 here), then across warps and CTAs in FP64.
+  __device__ bool sum1f(int slot, float a, double& out) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    double v[1] = {double(a)};
+    if (!sum<1, true>(slot, v)) return false;
+    out = v[0];
     return true;
   }
 };
@@ -468,8 +481,13 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
         pap_t = fma(p[i], api, pap_t);
       });
     }
-    double pap = double(pap_t);
-    if (!gs.sum1(1 + (k & 1), pap)) return;
+    double pap;
+    if constexpr (FUSE) {
+      if (!gs.sum1f(1 + (k & 1), float(pap_t), pap)) return;
+    } else {
+      pap = double(pap_t);
+      if (!gs.sum1(1 + (k & 1), pap)) return;
+    }
     const T dot = T(pap);
     if (!(dot > T(0)) || !isfinite(double(dot))) {
       if (tid == 0 && blockIdx.x == 0) atomicOr(P.status, kErrBreakdown);
@@ -497,8 +515,13 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
       r[i] = ri;
       rrn_t = fma(ri, ri, rrn_t);
     });
-    double rrn = double(rrn_t);
-    if (!gs.sum1(3, rrn)) return;
+    double rrn;
+    if constexpr (FUSE) {
+      if (!gs.sum1f(3, float(rrn_t), rrn)) return;
+    } else {
+      rrn = double(rrn_t);
+      if (!gs.sum1(3, rrn)) return;
+    }
     r0 = r1;
     r1 = T(rrn);
     k++;
@@ -593,8 +616,8 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
         pap_t = fmaf(pi, api, pap_t);
       });
     }
-    double pap = double(pap_t);
-    if (!gs.sum1(1 + (k & 1), pap)) return;
+    double pap;
+    if (!gs.sum1f(1 + (k & 1), pap_t, pap)) return;
     if (!(pap > 0.0) || !isfinite(pap)) {
       if (tid == 0 && blockIdx.x == 0) atomicOr(P.status, kErrBreakdown);
       return;
@@ -621,8 +644,8 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       r[i] = ri;
       rrn_t = fmaf(ri, ri, rrn_t);
     });
-    double rrn = double(rrn_t);
-    if (!gs.sum1(3, rrn)) return;
+    double rrn;
+    if (!gs.sum1f(3, rrn_t, rrn)) return;
     since++;
     const bool update = rrn < P.delta2 * maxrr || rrn < tol2 || (P.replace_every > 0 && since >= P.replace_every) ||
                         k == P.max_iter;
