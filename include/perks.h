@@ -211,6 +211,71 @@ PERKS_API int perks_spmv_csr(int dtype, int n, int nnz, const int* d_row_ptr, co
 PERKS_API int perks_spmv_dia(int dtype, int n, int ndiag, const int* h_offsets, const void* d_data,
                    const void* d_x, void* d_y, void* stream);
 
+/* ---------------------------------------------------------------- batches */
+/* Many independent stencil and CG instances of uneven size in ONE persistent
+ * launch: CTAs take whole jobs from a device work queue (largest first), so a
+ * job needs no grid-wide barrier; a stencil job whose two fields fit in one
+ * CTA's shared memory stays there for all its time steps. The run is a CUDA
+ * graph {reset the queue, launch}. The reference runs one instance per
+ * executable (stencil/2dstencil/jacobi.driver.cpp, conjugateGradient/
+ * cg_driver.cu); this interface has no counterpart there. */
+typedef enum { PERKS_JOB_STENCIL = 0, PERKS_JOB_CG = 1 } perks_job_kind;
+
+typedef struct {
+  int kind;          /* perks_job_kind */
+  int dtype;         /* PERKS_FP32 or PERKS_FP64 */
+  /* stencil: shape (PERKS_2D5PT, PERKS_2DS9PT, PERKS_2D9PT or PERKS_3D7PT),
+   * clamp boundary, reference evaluation order; h = 1 for 2D */
+  int shape, h, wy, wx, steps;
+  const void* d_in;  /* device field [h][wy][wx], not modified */
+  void* d_out;       /* device field [h][wy][wx] */
+  /* CG: A in CSR (device; values of dtype), b, x (device, dtype); x starts
+   * at 0 (its input is ignored); stop when ||r|| <= tol ||b|| or after
+   * max_iter iterations */
+  int n, nnz;
+  const int* d_row_ptr;
+  const int* d_col;
+  const void* d_val;
+  const void* d_b;
+  void* d_x;
+  double tol;
+  int max_iter;
+} perks_job;
+
+typedef struct {
+  int iterations;    /* CG: iterations done; stencil: time steps done */
+  int status;        /* PERKS_OK, or PERKS_ERR_BREAKDOWN / PERKS_ERR_NOT_CONVERGED for CG */
+  double rel_res;    /* CG: ||r|| / ||b|| of the recursive residual */
+} perks_job_result;
+
+typedef struct {
+  int threads;       /* threads per CTA (256, 512 or 1024); 0 = autotune */
+  int ctas_per_sm;   /* 1 or 2; 0 = autotune */
+  void* stream;      /* cudaStream_t; NULL = default stream */
+} perks_batch_opts;
+
+typedef struct {
+  double ms;          /* device time of the last run */
+  int threads, ctas_per_sm, grid;  /* the launch shape in use */
+  int resident_jobs;  /* stencil jobs kept in shared memory for all steps */
+  int tuned;          /* 1 if the launch shape came from the autotuner */
+} perks_batch_stats;
+
+typedef struct perks_batch_plan_s* perks_batch_plan;
+
+PERKS_API void perks_batch_default_opts(perks_batch_opts* opts);
+/* Validate the jobs, order them, allocate their scratch, autotune the launch
+ * shape when asked (by timing one run of each candidate), and capture the
+ * graph. Job pointers must stay valid while the plan exists. */
+PERKS_API int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_opts* opts,
+                                      perks_batch_plan* plan);
+/* Run the batch once (graph launch on `stream`, or the plan's stream when
+ * NULL) and wait for it; stats may be NULL. */
+PERKS_API int perks_batch_plan_run(perks_batch_plan plan, void* stream, perks_batch_stats* stats);
+/* Per-job results of the last run, in the caller's job order (njobs entries). */
+PERKS_API int perks_batch_plan_results(perks_batch_plan plan, perks_job_result* results);
+PERKS_API void perks_batch_plan_destroy(perks_batch_plan plan);
+
 /* ------------------------------------------------------------------ misc */
 PERKS_API const char* perks_last_error(void);     /* thread-local message of the last failure */
 PERKS_API const char* perks_status_string(int status);

@@ -8,9 +8,11 @@ from . import _native
 from ._native import PerksError, SHAPES, HALO, lib
 from .stencil import j3d_iterative, jacobi_iterative, last_error, stencil2d, stencil3d
 from .cg import cg_csr, cg_dia, spmv_csr, spmv_dia
+from .batch import BatchPlan, cg_job, stencil_job
 
 __all__ = ["PerksError", "SHAPES", "HALO", "lib", "jacobi_iterative", "j3d_iterative", "stencil2d",
-           "stencil3d", "last_error", "cg_csr", "cg_dia", "spmv_csr", "spmv_dia"]
+           "stencil3d", "last_error", "cg_csr", "cg_dia", "spmv_csr", "spmv_dia", "BatchPlan", "cg_job",
+           "stencil_job"]
 
 
 def launch_count() -> int:

@@ -56,6 +56,28 @@ class CgResult(ctypes.Structure):
                 ("ms", c_double), ("launches", c_int)]
 
 
+class Job(ctypes.Structure):
+    _fields_ = [("kind", c_int), ("dtype", c_int), ("shape", c_int), ("h", c_int), ("wy", c_int), ("wx", c_int),
+                ("steps", c_int), ("d_in", c_void_p), ("d_out", c_void_p), ("n", c_int), ("nnz", c_int),
+                ("d_row_ptr", c_void_p), ("d_col", c_void_p), ("d_val", c_void_p), ("d_b", c_void_p),
+                ("d_x", c_void_p), ("tol", c_double), ("max_iter", c_int)]
+
+
+class JobResult(ctypes.Structure):
+    _fields_ = [("iterations", c_int), ("status", c_int), ("rel_res", c_double)]
+
+
+class BatchOpts(ctypes.Structure):
+    _fields_ = [("threads", c_int), ("ctas_per_sm", c_int), ("stream", c_void_p)]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [("ms", c_double), ("threads", c_int), ("ctas_per_sm", c_int), ("grid", c_int),
+                ("resident_jobs", c_int), ("tuned", c_int)]
+
+
+JOB_STENCIL, JOB_CG = 0, 1
+
 # Every function the header declares, with its ctypes signature.
 SIGNATURES = {
     "perks_stencil_default_opts": (None, [ctypes.POINTER(StencilOpts), c_int, c_int]),
@@ -77,6 +99,12 @@ SIGNATURES = {
     "perks_spmv_csr": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                c_void_p]),
     "perks_spmv_dia": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "perks_batch_default_opts": (None, [ctypes.POINTER(BatchOpts)]),
+    "perks_batch_plan_create": (c_int, [ctypes.POINTER(Job), c_int, ctypes.POINTER(BatchOpts),
+                                        ctypes.POINTER(c_void_p)]),
+    "perks_batch_plan_run": (c_int, [c_void_p, c_void_p, ctypes.POINTER(BatchStats)]),
+    "perks_batch_plan_results": (c_int, [c_void_p, ctypes.POINTER(JobResult)]),
+    "perks_batch_plan_destroy": (None, [c_void_p]),
     "perks_last_error": (ctypes.c_char_p, []),
     "perks_status_string": (ctypes.c_char_p, [c_int]),
     "perks_abi_version": (c_int, []),

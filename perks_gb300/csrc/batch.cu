@@ -1,0 +1,476 @@
+// Batched uneven workload in one persistent launch.
+//
+// The jobs (independent stencil time loops and CG solves of different sizes
+// and precisions) are ordered largest first into a device job table. Every
+// CTA of one launch repeatedly takes the next job from an atomic counter and
+// runs the whole job alone, so a job needs only CTA barriers, never a grid
+// barrier, and big jobs start first while small ones fill the tail.
+//   * Stencil job: if both fields fit in the CTA's shared memory they stay
+//     there for every time step (the PERKS idea taken to the whole domain);
+//     otherwise the CTA ping-pongs between the output and a scratch field in
+//     global memory (L2-resident for these sizes). Clamp boundary, reference
+//     evaluation order: results are bit-identical to the single-instance path
+//     and to the reference CPU code.
+//   * CG job: CSR, x0 = 0, CTA-wide reductions, stop at ||r|| <= tol ||b||.
+// A run is a CUDA graph of {reset the counter, launch}; the launch shape
+// (threads per CTA, CTAs per SM, hence shared memory per CTA) is chosen by
+// timing each candidate once when the plan is created.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+#include "ptx.cuh"
+#include "runtime.cuh"
+#include "shapes.cuh"
+
+namespace perks {
+
+struct BJob {  // one job, in queue order
+  int kind, dtype, shape, h, wy, wx, steps;
+  const void* in;
+  void* out;
+  void* scratch;  // stencil: second field; CG: r, p, Ap
+  int n, nnz;
+  const int* rp;
+  const int* ci;
+  const void* val;
+  const void* b;
+  void* x;
+  double tol;
+  int max_iter;
+};
+struct BRes {
+  int iterations, status;
+  double rel_res;
+};
+
+// CTA-wide sum of one double, valid in every thread (`red`: 32 doubles).
+__device__ __forceinline__ double cta_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  v = lane < nw ? red[lane] : 0.0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <class T, int SHAPE>
+__device__ void batch_stencil(const BJob& J, unsigned char* smem, unsigned smem_bytes, BRes* res) {
+  const int h = J.h, wy = J.wy, wx = J.wx, steps = J.steps;
+  const long long cells = (long long)h * wy * wx;
+  const int nt = blockDim.x, tid = threadIdx.x;
+  // threads per row (whole warps), rows in parallel
+  const int tpr = min(nt, ((wx + 31) / 32) * 32);
+  const int rpar = nt / tpr;
+  const int r_off = tid / tpr, c0 = tid % tpr;
+  const int rows = h * wy;
+  auto sweep = [&](const T* __restrict__ src, T* __restrict__ dst) {
+    if (r_off >= rpar) return;
+    for (int row = r_off; row < rows; row += rpar) {
+      const int z = row / wy, y = row - z * wy;
+      for (int x = c0; x < wx; x += tpr) {
+        auto u = [&](int dz, int dy, int dx) -> T {
+          const int zz = min(max(z + dz, 0), h - 1), yy = min(max(y + dy, 0), wy - 1), xx = min(max(x + dx, 0), wx - 1);
+          return src[((size_t)zz * wy + yy) * wx + xx];
+        };
+        dst[((size_t)z * wy + y) * wx + x] = stencil_point<T, SHAPE, false>(u);
+      }
+    }
+  };
+  const T* in = static_cast<const T*>(J.in);
+  T* out = static_cast<T*>(J.out);
+  if (steps == 0) {
+    for (long long i = tid; i < cells; i += nt) out[i] = in[i];
+  } else if (2 * cells * (long long)sizeof(T) <= (long long)smem_bytes) {
+    T* A = reinterpret_cast<T*>(smem);
+    T* B = A + cells;
+    for (long long i = tid; i < cells; i += nt) A[i] = in[i];
+    __syncthreads();
+    for (int t = 0; t < steps; t++) {
+      sweep(A, B);
+      __syncthreads();
+      T* tmp = A;
+      A = B;
+      B = tmp;
+    }
+    for (long long i = tid; i < cells; i += nt) out[i] = A[i];
+  } else {
+    T* scratch = static_cast<T*>(J.scratch);
+    const T* src = in;
+    for (int t = 0; t < steps; t++) {
+      T* dst = ((steps - 1 - t) & 1) == 0 ? out : scratch;  // the last step writes `out`
+      sweep(src, dst);
+      __syncthreads();  // this CTA's global writes are visible to it after the barrier
+      src = dst;
+    }
+  }
+  if (tid == 0) {
+    res->iterations = steps;
+    res->status = PERKS_OK;
+    res->rel_res = 0.0;
+  }
+}
+
+template <class T>
+__device__ void batch_cg(const BJob& J, double* red, BRes* res) {
+  const int n = J.n, nt = blockDim.x, tid = threadIdx.x;
+  const int* __restrict__ rp = J.rp;
+  const int* __restrict__ ci = J.ci;
+  const T* __restrict__ val = static_cast<const T*>(J.val);
+  const T* __restrict__ b = static_cast<const T*>(J.b);
+  T* __restrict__ x = static_cast<T*>(J.x);
+  T* __restrict__ r = static_cast<T*>(J.scratch);
+  T* __restrict__ p = r + ((n + 63) & ~63);
+  T* __restrict__ Ap = p + ((n + 63) & ~63);
+  double rr = 0.0;
+  for (int i = tid; i < n; i += nt) {
+    const T bi = b[i];
+    x[i] = T(0);
+    r[i] = bi;
+    p[i] = bi;
+    rr += double(bi) * double(bi);
+  }
+  rr = cta_sum(rr, red);
+  const double bb = rr, stop2 = J.tol * J.tol * bb;
+  int k = 0, status = PERKS_OK;
+  while (k < J.max_iter && rr > stop2) {
+    __syncthreads();  // p complete before the SpMV gathers it
+    double pap = 0.0;
+    for (int i = tid; i < n; i += nt) {
+      T acc = T(0);
+      for (int j = rp[i]; j < rp[i + 1]; j++) acc = fma(val[j], p[ci[j]], acc);
+      Ap[i] = acc;
+      pap += double(p[i]) * double(acc);
+    }
+    pap = cta_sum(pap, red);
+    if (!(pap > 0.0) || !isfinite(pap)) {
+      status = PERKS_ERR_BREAKDOWN;
+      break;
+    }
+    const T alpha = T(rr / pap);
+    double rrn = 0.0;
+    for (int i = tid; i < n; i += nt) {
+      x[i] = fma(alpha, p[i], x[i]);
+      const T ri = fma(-alpha, Ap[i], r[i]);
+      r[i] = ri;
+      rrn += double(ri) * double(ri);
+    }
+    rrn = cta_sum(rrn, red);
+    const T beta = T(rrn / rr);
+    for (int i = tid; i < n; i += nt) p[i] = fma(beta, p[i], r[i]);
+    rr = rrn;
+    k++;
+  }
+  if (status == PERKS_OK && rr > stop2) status = PERKS_ERR_NOT_CONVERGED;
+  if (tid == 0) {
+    res->iterations = k;
+    res->status = status;
+    res->rel_res = bb > 0.0 ? sqrt(rr / bb) : sqrt(rr);
+  }
+}
+
+__global__ void __launch_bounds__(1024, 1)
+    batch_kernel(const BJob* __restrict__ jobs, int njobs, BRes* res, unsigned* counter, unsigned smem_bytes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int sj;
+  __shared__ double red[32];
+  while (true) {
+    if (threadIdx.x == 0) sj = int(atomicAdd(counter, 1u));
+    __syncthreads();
+    const int j = sj;
+    if (j >= njobs) break;
+    const BJob& J = jobs[j];
+    const bool f64 = J.dtype == PERKS_FP64;
+    if (J.kind == PERKS_JOB_CG) {
+      if (f64) batch_cg<double>(J, red, res + j);
+      else batch_cg<float>(J, red, res + j);
+    } else {
+      switch (J.shape) {
+        case PERKS_2D5PT:
+          if (f64) batch_stencil<double, PERKS_2D5PT>(J, smem, smem_bytes, res + j);
+          else batch_stencil<float, PERKS_2D5PT>(J, smem, smem_bytes, res + j);
+          break;
+        case PERKS_2DS9PT:
+          if (f64) batch_stencil<double, PERKS_2DS9PT>(J, smem, smem_bytes, res + j);
+          else batch_stencil<float, PERKS_2DS9PT>(J, smem, smem_bytes, res + j);
+          break;
+        case PERKS_2D9PT:
+          if (f64) batch_stencil<double, PERKS_2D9PT>(J, smem, smem_bytes, res + j);
+          else batch_stencil<float, PERKS_2D9PT>(J, smem, smem_bytes, res + j);
+          break;
+        default:  // PERKS_3D7PT (validated on the host)
+          if (f64) batch_stencil<double, PERKS_3D7PT>(J, smem, smem_bytes, res + j);
+          else batch_stencil<float, PERKS_3D7PT>(J, smem, smem_bytes, res + j);
+          break;
+      }
+    }
+    __syncthreads();  // every thread has read sj before it is overwritten
+  }
+}
+
+}  // namespace perks
+
+using namespace perks;
+
+struct perks_batch_plan_s {
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  int njobs = 0;
+  std::vector<int> order;  // queue position -> caller's index
+  std::vector<long long> cells_of;  // per queue position, stencil cells x sizeof (0 for CG)
+  BJob* d_jobs = nullptr;
+  BRes* d_res = nullptr;
+  unsigned* d_counter = nullptr;
+  void* d_scratch = nullptr;
+  int threads = 0, ctas_per_sm = 0, grid = 0, tuned = 0, resident = 0;
+  unsigned smem = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  float last_ms = 0.f;
+};
+
+namespace {
+
+bool batch_shape_ok(int s) {
+  return s == PERKS_2D5PT || s == PERKS_2DS9PT || s == PERKS_2D9PT || s == PERKS_3D7PT;
+}
+
+void plan_free(perks_batch_plan p) {
+  if (!p) return;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  if (p->e0) cudaEventDestroy(p->e0);
+  if (p->e1) cudaEventDestroy(p->e1);
+  cudaFree(p->d_jobs);
+  cudaFree(p->d_res);
+  cudaFree(p->d_counter);
+  cudaFree(p->d_scratch);
+  delete p;
+}
+
+// Shared memory per CTA for a launch shape (dynamic part).
+unsigned smem_for(const DeviceInfo* dev, int ctas_per_sm) {
+  const size_t per_sm = 228 * 1024;  // GB300 shared memory per SM
+  size_t s = per_sm / size_t(ctas_per_sm) - 1024 - 512;  // CTA reservation + static smem
+  return unsigned(std::min(s, dev->smem_optin));
+}
+
+int launch_once(perks_batch_plan p, cudaStream_t s, int threads, int ctas, unsigned smem, float* ms) {
+  PERKS_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  const int grid = device_info()->sms * ctas;
+  PERKS_CUDA(cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned), s));
+  PERKS_CUDA(cudaEventRecord(p->e0, s));
+  batch_kernel<<<grid, threads, smem, s>>>(p->d_jobs, p->njobs, p->d_res, p->d_counter, smem);
+  PERKS_CUDA(cudaGetLastError());
+  PERKS_CUDA(cudaEventRecord(p->e1, s));
+  PERKS_CUDA(cudaEventSynchronize(p->e1));
+  count_launch(1);
+  PERKS_CUDA(cudaEventElapsedTime(ms, p->e0, p->e1));
+  return PERKS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void perks_batch_default_opts(perks_batch_opts* o) {
+  if (!o) return;
+  *o = perks_batch_opts{};
+}
+
+int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_opts* opts, perks_batch_plan* out) {
+  if (!out) return fail(PERKS_ERR_INVALID_ARG, "plan is NULL");
+  *out = nullptr;
+  if (!jobs || njobs <= 0) return fail(PERKS_ERR_INVALID_ARG, "no jobs");
+  perks_batch_opts o{};
+  if (opts) o = *opts;
+  if (o.threads != 0 && o.threads != 256 && o.threads != 512 && o.threads != 1024)
+    return fail(PERKS_ERR_INVALID_ARG, "threads must be 0, 256, 512 or 1024");
+  if (o.ctas_per_sm < 0 || o.ctas_per_sm > 2) return fail(PERKS_ERR_INVALID_ARG, "ctas_per_sm must be 0, 1 or 2");
+  const DeviceInfo* dev = device_info();
+  if (!dev) return PERKS_ERR_NO_DEVICE;
+
+  // validate; cost estimate for the order
+  std::vector<double> cost(njobs);
+  std::vector<size_t> scratch_bytes(njobs);
+  for (int i = 0; i < njobs; i++) {
+    const perks_job& J = jobs[i];
+    const std::string at = "job " + std::to_string(i) + ": ";
+    if (J.dtype != PERKS_FP32 && J.dtype != PERKS_FP64) return fail(PERKS_ERR_INVALID_ARG, at + "dtype");
+    const size_t es = J.dtype == PERKS_FP64 ? 8 : 4;
+    if (J.kind == PERKS_JOB_STENCIL) {
+      if (!batch_shape_ok(J.shape))
+        return fail(PERKS_ERR_UNSUPPORTED, at + "batched stencils are 2d5pt, 2ds9pt, 2d9pt and 3d7pt");
+      const bool is3d = J.shape == PERKS_3D7PT;
+      if (J.h <= 0 || J.wy <= 0 || J.wx <= 0 || J.steps < 0 || (!is3d && J.h != 1))
+        return fail(PERKS_ERR_INVALID_ARG, at + "bad stencil size");
+      if (!J.d_in || !J.d_out) return fail(PERKS_ERR_INVALID_ARG, at + "NULL field");
+      const double cells = double(J.h) * J.wy * J.wx;
+      if (cells > 2e9) return fail(PERKS_ERR_UNSUPPORTED, at + "field too large for one CTA");
+      cost[i] = cells * std::max(J.steps, 1) * (J.dtype == PERKS_FP64 ? 8.0 : 1.0);
+      scratch_bytes[i] = (size_t(cells) * es + 255) & ~size_t(255);
+    } else if (J.kind == PERKS_JOB_CG) {
+      if (J.n <= 0 || J.nnz < 0 || !J.d_row_ptr || !J.d_col || !J.d_val || !J.d_b || !J.d_x)
+        return fail(PERKS_ERR_INVALID_ARG, at + "bad CSR arguments");
+      if (J.max_iter < 0 || !(J.tol >= 0)) return fail(PERKS_ERR_INVALID_ARG, at + "bad max_iter or tol");
+      cost[i] = double(J.nnz + J.n) * std::sqrt(double(J.n)) * 4.0 * (J.dtype == PERKS_FP64 ? 4.0 : 1.0);
+      scratch_bytes[i] = 3 * ((size_t((J.n + 63) & ~63) * es + 255) & ~size_t(255));
+    } else {
+      return fail(PERKS_ERR_INVALID_ARG, at + "unknown job kind");
+    }
+  }
+  perks_batch_plan p = new perks_batch_plan_s();
+  p->device = dev->device;
+  p->stream = static_cast<cudaStream_t>(o.stream);
+  p->njobs = njobs;
+  p->order.resize(njobs);
+  for (int i = 0; i < njobs; i++) p->order[i] = i;
+  std::stable_sort(p->order.begin(), p->order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+
+  size_t total = 0;
+  std::vector<size_t> offs(njobs);
+  for (int q = 0; q < njobs; q++) {
+    offs[q] = total;
+    total += scratch_bytes[p->order[q]];
+  }
+  auto bail = [&](int rc) {
+    plan_free(p);
+    return rc;
+  };
+  cudaError_t e;
+  if ((e = cudaMalloc(&p->d_scratch, std::max<size_t>(total, 256))) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaMalloc(batch scratch)"));
+  if ((e = cudaMalloc(&p->d_jobs, sizeof(BJob) * njobs)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(jobs)"));
+  if ((e = cudaMalloc(&p->d_res, sizeof(BRes) * njobs)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(results)"));
+  if ((e = cudaMalloc(&p->d_counter, 256)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(counter)"));
+  if ((e = cudaEventCreate(&p->e0)) != cudaSuccess || (e = cudaEventCreate(&p->e1)) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaEventCreate"));
+
+  std::vector<BJob> table(njobs);
+  p->cells_of.assign(njobs, 0);
+  for (int q = 0; q < njobs; q++) {
+    const perks_job& J = jobs[p->order[q]];
+    BJob& B = table[q];
+    B = BJob{};
+    B.kind = J.kind;
+    B.dtype = J.dtype;
+    B.scratch = static_cast<unsigned char*>(p->d_scratch) + offs[q];
+    if (J.kind == PERKS_JOB_STENCIL) {
+      B.shape = J.shape;
+      B.h = J.h;
+      B.wy = J.wy;
+      B.wx = J.wx;
+      B.steps = J.steps;
+      B.in = J.d_in;
+      B.out = J.d_out;
+      p->cells_of[q] = (long long)J.h * J.wy * J.wx * (J.dtype == PERKS_FP64 ? 8 : 4);
+    } else {
+      B.n = J.n;
+      B.nnz = J.nnz;
+      B.rp = J.d_row_ptr;
+      B.ci = J.d_col;
+      B.val = J.d_val;
+      B.b = J.d_b;
+      B.x = J.d_x;
+      B.tol = J.tol;
+      B.max_iter = J.max_iter;
+    }
+  }
+  if ((e = cudaMemcpy(p->d_jobs, table.data(), sizeof(BJob) * njobs, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaMemcpy(jobs)"));
+
+  // launch shape: the caller's, or the fastest candidate of one timed run each
+  std::vector<std::pair<int, int>> cand;
+  for (int t : {256, 512, 1024})
+    for (int c : {1, 2})
+      if ((o.threads == 0 || o.threads == t) && (o.ctas_per_sm == 0 || o.ctas_per_sm == c) && t * c <= 1024)
+        cand.push_back({t, c});  // <= 1024 threads per SM: 64 registers per thread fit
+  if (cand.empty()) return bail(fail(PERKS_ERR_INVALID_ARG, "threads x ctas_per_sm must be <= 1024"));
+  float best = 1e30f;
+  if (cand.size() > 1) {  // warm-up (module load, cold L2) before the timed candidates
+    float ms = 0.f;
+    int rc = launch_once(p, p->stream, cand[0].first, cand[0].second, smem_for(dev, cand[0].second), &ms);
+    if (rc != PERKS_OK) return bail(rc);
+  }
+  for (auto& tc : cand) {
+    float ms = 0.f;
+    int rc = launch_once(p, p->stream, tc.first, tc.second, smem_for(dev, tc.second), &ms);
+    if (rc != PERKS_OK) return bail(rc);
+    if (cand.size() == 1 || ms < best) {
+      best = ms;
+      p->threads = tc.first;
+      p->ctas_per_sm = tc.second;
+    }
+  }
+  p->tuned = cand.size() > 1;
+  p->smem = smem_for(dev, p->ctas_per_sm);
+  p->grid = dev->sms * p->ctas_per_sm;
+  p->resident = 0;
+  for (int q = 0; q < njobs; q++)
+    if (p->cells_of[q] > 0 && 2 * p->cells_of[q] <= (long long)p->smem) p->resident++;
+
+  // the run as a graph: reset the queue counter, launch
+  if ((e = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(p->smem))) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaFuncSetAttribute(batch)"));
+  cudaStream_t cs;
+  if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaStreamCreate"));
+  e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned), cs);
+    batch_kernel<<<p->grid, p->threads, p->smem, cs>>>(p->d_jobs, p->njobs, p->d_res, p->d_counter, p->smem);
+    e = cudaStreamEndCapture(cs, &p->graph);
+  }
+  cudaStreamDestroy(cs);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "graph capture (batch)"));
+  if ((e = cudaGraphInstantiate(&p->exec, p->graph, 0)) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaGraphInstantiate(batch)"));
+  p->last_ms = best;
+  *out = p;
+  return PERKS_OK;
+}
+
+int perks_batch_plan_run(perks_batch_plan p, void* stream, perks_batch_stats* st) {
+  if (!p) return fail(PERKS_ERR_INVALID_ARG, "plan is NULL");
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : p->stream;
+  PERKS_CUDA(cudaEventRecord(p->e0, s));
+  PERKS_CUDA(cudaGraphLaunch(p->exec, s));
+  PERKS_CUDA(cudaEventRecord(p->e1, s));
+  PERKS_CUDA(cudaEventSynchronize(p->e1));
+  count_launch(1);
+  float ms = 0.f;
+  PERKS_CUDA(cudaEventElapsedTime(&ms, p->e0, p->e1));
+  p->last_ms = ms;
+  if (st) {
+    st->ms = ms;
+    st->threads = p->threads;
+    st->ctas_per_sm = p->ctas_per_sm;
+    st->grid = p->grid;
+    st->resident_jobs = p->resident;
+    st->tuned = p->tuned;
+  }
+  return PERKS_OK;
+}
+
+int perks_batch_plan_results(perks_batch_plan p, perks_job_result* results) {
+  if (!p || !results) return fail(PERKS_ERR_INVALID_ARG, "plan or results is NULL");
+  std::vector<BRes> r(p->njobs);
+  PERKS_CUDA(cudaMemcpy(r.data(), p->d_res, sizeof(BRes) * p->njobs, cudaMemcpyDeviceToHost));
+  for (int q = 0; q < p->njobs; q++) {
+    perks_job_result& o = results[p->order[q]];
+    o.iterations = r[q].iterations;
+    o.status = r[q].status;
+    o.rel_res = r[q].rel_res;
+  }
+  return PERKS_OK;
+}
+
+void perks_batch_plan_destroy(perks_batch_plan p) { plan_free(p); }
+
+}  // extern "C"
