@@ -213,8 +213,10 @@ PERKS_API int perks_spmv_dia(int dtype, int n, int ndiag, const int* h_offsets, 
 
 /* ---------------------------------------------------------------- batches */
 /* Many independent stencil and CG instances of uneven size in ONE persistent
- * launch: CTAs take whole jobs from a device work queue (largest first), so a
- * job needs no grid-wide barrier; a stencil job whose two fields fit in one
+ * launch: CTAs take work items from a device work queue (largest jobs first).
+ * A job is one item, or, for a stencil job larger than total work / (2 x SMs),
+ * a run of row slices whose CTAs meet at a job barrier after each time step;
+ * no grid-wide barrier is used. A stencil job whose two fields fit in one
  * CTA's shared memory stays there for all its time steps. The run is a CUDA
  * graph {reset the queue, launch}. The reference runs one instance per
  * executable (stencil/2dstencil/jacobi.driver.cpp, conjugateGradient/
@@ -259,6 +261,7 @@ typedef struct {
   int threads, ctas_per_sm, grid;  /* the launch shape in use */
   int resident_jobs;  /* stencil jobs kept in shared memory for all steps */
   int tuned;          /* 1 if the launch shape came from the autotuner */
+  int sliced_jobs;    /* stencil jobs cut into row slices run by several CTAs */
 } perks_batch_stats;
 
 typedef struct perks_batch_plan_s* perks_batch_plan;

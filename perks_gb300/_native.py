@@ -73,7 +73,7 @@ class BatchOpts(ctypes.Structure):
 
 class BatchStats(ctypes.Structure):
     _fields_ = [("ms", c_double), ("threads", c_int), ("ctas_per_sm", c_int), ("grid", c_int),
-                ("resident_jobs", c_int), ("tuned", c_int)]
+                ("resident_jobs", c_int), ("tuned", c_int), ("sliced_jobs", c_int)]
 
 
 JOB_STENCIL, JOB_CG = 0, 1

@@ -1,10 +1,16 @@
 // Batched uneven workload in one persistent launch.
 //
 // The jobs (independent stencil time loops and CG solves of different sizes
-// and precisions) are ordered largest first into a device job table. Every
-// CTA of one launch repeatedly takes the next job from an atomic counter and
-// runs the whole job alone, so a job needs only CTA barriers, never a grid
-// barrier, and big jobs start first while small ones fill the tail.
+// and precisions) are ordered largest first. A stencil job larger than the
+// balancing unit (total work / (2 x SMs)) is cut into row slices, the rest is
+// one work item each; the items go into a device queue in that order. Every
+// CTA of one launch repeatedly takes the next item from an atomic counter. A
+// single-item job needs only CTA barriers; the CTAs holding the slices of one
+// job meet at a job barrier (monotonic counter, bounded wait) after every
+// time step and read neighbouring rows through L2 (ld.global.cg). This cannot
+// deadlock: the grid is fully resident, and a job's slices are consecutive in
+// the queue, so by the time any later job's item is taken every slice of every
+// earlier job is held by a running CTA.
 //   * Stencil job: if both fields fit in the CTA's shared memory they stay
 //     there for every time step (the PERKS idea taken to the whole domain);
 //     otherwise the CTA ping-pongs between the output and a scratch field in
@@ -44,6 +50,33 @@ struct BRes {
   int iterations, status;
   double rel_res;
 };
+struct BItem {  // one work item: a job, or one row slice of a stencil job
+  int job, slice, nslices, row_lo, row_hi;
+};
+
+// Barrier of the nslices CTAs working on one job: monotonic counter, target
+// = (steps done) x nslices. False when the wait ran out its budget.
+__device__ __forceinline__ bool job_barrier(unsigned* bar, unsigned target) {
+  __shared__ unsigned s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned ok = 1, old;
+    __threadfence();
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(bar) : "memory");
+    if (int(old + 1u - target) < 0) {
+      const long long t0 = clock64();
+      while (int(ld_acquire_gpu(bar) - target) < 0) {
+        if (clock64() - t0 > kWaitBudget) {
+          ok = 0;
+          break;
+        }
+      }
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
 
 // CTA-wide sum of one double, valid in every thread (`red`: 32 doubles).
 __device__ __forceinline__ double cta_sum(double v, double* red) {
@@ -59,29 +92,61 @@ __device__ __forceinline__ double cta_sum(double v, double* red) {
   return v;
 }
 
-template <class T, int SHAPE>
-__device__ void batch_stencil(const BJob& J, unsigned char* smem, unsigned smem_bytes, BRes* res) {
-  const int h = J.h, wy = J.wy, wx = J.wx, steps = J.steps;
-  const long long cells = (long long)h * wy * wx;
+// One time step over rows [r_lo, r_hi) of the job's (h*wy) rows. L2 = true
+// reads through L2 only (other CTAs wrote the source).
+template <class T, int SHAPE, bool L2>
+__device__ __forceinline__ void stencil_rows(const BJob& J, const T* __restrict__ src, T* __restrict__ dst, int r_lo,
+                                             int r_hi) {
+  const int h = J.h, wy = J.wy, wx = J.wx;
   const int nt = blockDim.x, tid = threadIdx.x;
   // threads per row (whole warps), rows in parallel
   const int tpr = min(nt, ((wx + 31) / 32) * 32);
   const int rpar = nt / tpr;
   const int r_off = tid / tpr, c0 = tid % tpr;
-  const int rows = h * wy;
-  auto sweep = [&](const T* __restrict__ src, T* __restrict__ dst) {
-    if (r_off >= rpar) return;
-    for (int row = r_off; row < rows; row += rpar) {
-      const int z = row / wy, y = row - z * wy;
-      for (int x = c0; x < wx; x += tpr) {
-        auto u = [&](int dz, int dy, int dx) -> T {
-          const int zz = min(max(z + dz, 0), h - 1), yy = min(max(y + dy, 0), wy - 1), xx = min(max(x + dx, 0), wx - 1);
-          return src[((size_t)zz * wy + yy) * wx + xx];
-        };
-        dst[((size_t)z * wy + y) * wx + x] = stencil_point<T, SHAPE, false>(u);
-      }
+  if (r_off >= rpar) return;
+  for (int row = r_lo + r_off; row < r_hi; row += rpar) {
+    const int z = row / wy, y = row - z * wy;
+    for (int x = c0; x < wx; x += tpr) {
+      auto u = [&](int dz, int dy, int dx) -> T {
+        const int zz = min(max(z + dz, 0), h - 1), yy = min(max(y + dy, 0), wy - 1), xx = min(max(x + dx, 0), wx - 1);
+        const T* a = src + ((size_t)zz * wy + yy) * wx + xx;
+        if constexpr (L2) return __ldcg(a);
+        else return *a;
+      };
+      dst[((size_t)z * wy + y) * wx + x] = stencil_point<T, SHAPE, false>(u);
     }
-  };
+  }
+}
+
+// A stencil job cut into nslices row slices, this CTA holding one of them.
+template <class T, int SHAPE>
+__device__ void batch_stencil_slice(const BJob& J, const BItem& I, unsigned* bar, BRes* res) {
+  const int steps = J.steps;
+  const T* src = static_cast<const T*>(J.in);
+  T* out = static_cast<T*>(J.out);
+  T* scratch = static_cast<T*>(J.scratch);
+  int done = 0;
+  for (int t = 0; t < steps; t++) {
+    T* dst = ((steps - 1 - t) & 1) == 0 ? out : scratch;  // the last step writes `out`
+    stencil_rows<T, SHAPE, true>(J, src, dst, I.row_lo, I.row_hi);
+    if (!job_barrier(bar, unsigned(t + 1) * unsigned(I.nslices))) break;
+    src = dst;
+    done = t + 1;
+  }
+  if (I.slice == 0 && threadIdx.x == 0) {
+    res->iterations = done;
+    res->status = done == steps ? PERKS_OK : PERKS_ERR_TIMEOUT;
+    res->rel_res = 0.0;
+  }
+}
+
+template <class T, int SHAPE>
+__device__ void batch_stencil(const BJob& J, unsigned char* smem, unsigned smem_bytes, BRes* res) {
+  const int h = J.h, wy = J.wy, wx = J.wx, steps = J.steps;
+  const long long cells = (long long)h * wy * wx;
+  const int nt = blockDim.x, tid = threadIdx.x;
+  const int rows = h * wy;
+  auto sweep = [&](const T* __restrict__ src, T* __restrict__ dst) { stencil_rows<T, SHAPE, false>(J, src, dst, 0, rows); };
   const T* in = static_cast<const T*>(J.in);
   T* out = static_cast<T*>(J.out);
   if (steps == 0) {
@@ -174,19 +239,43 @@ __device__ void batch_cg(const BJob& J, double* red, BRes* res) {
   }
 }
 
+// counter[0]: the queue; counter[1 + job]: the job barriers (all zero at launch)
 __global__ void __launch_bounds__(1024, 1)
-    batch_kernel(const BJob* __restrict__ jobs, int njobs, BRes* res, unsigned* counter, unsigned smem_bytes) {
+    batch_kernel(const BJob* __restrict__ jobs, const BItem* __restrict__ items, int nitems, BRes* res,
+                 unsigned* counter, unsigned smem_bytes) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ int sj;
+  __shared__ int sq;
   __shared__ double red[32];
   while (true) {
-    if (threadIdx.x == 0) sj = int(atomicAdd(counter, 1u));
+    if (threadIdx.x == 0) sq = int(atomicAdd(counter, 1u));
     __syncthreads();
-    const int j = sj;
-    if (j >= njobs) break;
+    const int q = sq;
+    if (q >= nitems) break;
+    const BItem I = items[q];
+    const int j = I.job;
     const BJob& J = jobs[j];
     const bool f64 = J.dtype == PERKS_FP64;
-    if (J.kind == PERKS_JOB_CG) {
+    if (I.nslices > 1) {
+      unsigned* bar = counter + 1 + j;
+      switch (J.shape) {
+        case PERKS_2D5PT:
+          if (f64) batch_stencil_slice<double, PERKS_2D5PT>(J, I, bar, res + j);
+          else batch_stencil_slice<float, PERKS_2D5PT>(J, I, bar, res + j);
+          break;
+        case PERKS_2DS9PT:
+          if (f64) batch_stencil_slice<double, PERKS_2DS9PT>(J, I, bar, res + j);
+          else batch_stencil_slice<float, PERKS_2DS9PT>(J, I, bar, res + j);
+          break;
+        case PERKS_2D9PT:
+          if (f64) batch_stencil_slice<double, PERKS_2D9PT>(J, I, bar, res + j);
+          else batch_stencil_slice<float, PERKS_2D9PT>(J, I, bar, res + j);
+          break;
+        default:
+          if (f64) batch_stencil_slice<double, PERKS_3D7PT>(J, I, bar, res + j);
+          else batch_stencil_slice<float, PERKS_3D7PT>(J, I, bar, res + j);
+          break;
+      }
+    } else if (J.kind == PERKS_JOB_CG) {
       if (f64) batch_cg<double>(J, red, res + j);
       else batch_cg<float>(J, red, res + j);
     } else {
@@ -209,7 +298,7 @@ __global__ void __launch_bounds__(1024, 1)
           break;
       }
     }
-    __syncthreads();  // every thread has read sj before it is overwritten
+    __syncthreads();  // every thread has read sq before it is overwritten
   }
 }
 
@@ -224,6 +313,8 @@ struct perks_batch_plan_s {
   std::vector<int> order;  // queue position -> caller's index
   std::vector<long long> cells_of;  // per queue position, stencil cells x sizeof (0 for CG)
   BJob* d_jobs = nullptr;
+  BItem* d_items = nullptr;
+  int nitems = 0, sliced = 0;
   BRes* d_res = nullptr;
   unsigned* d_counter = nullptr;
   void* d_scratch = nullptr;
@@ -248,6 +339,7 @@ void plan_free(perks_batch_plan p) {
   if (p->e0) cudaEventDestroy(p->e0);
   if (p->e1) cudaEventDestroy(p->e1);
   cudaFree(p->d_jobs);
+  cudaFree(p->d_items);
   cudaFree(p->d_res);
   cudaFree(p->d_counter);
   cudaFree(p->d_scratch);
@@ -264,9 +356,9 @@ unsigned smem_for(const DeviceInfo* dev, int ctas_per_sm) {
 int launch_once(perks_batch_plan p, cudaStream_t s, int threads, int ctas, unsigned smem, float* ms) {
   PERKS_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   const int grid = device_info()->sms * ctas;
-  PERKS_CUDA(cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned), s));
+  PERKS_CUDA(cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned) * (1 + p->njobs), s));
   PERKS_CUDA(cudaEventRecord(p->e0, s));
-  batch_kernel<<<grid, threads, smem, s>>>(p->d_jobs, p->njobs, p->d_res, p->d_counter, smem);
+  batch_kernel<<<grid, threads, smem, s>>>(p->d_jobs, p->d_items, p->nitems, p->d_res, p->d_counter, smem);
   PERKS_CUDA(cudaGetLastError());
   PERKS_CUDA(cudaEventRecord(p->e1, s));
   PERKS_CUDA(cudaEventSynchronize(p->e1));
@@ -348,7 +440,8 @@ int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_
     return bail(cuda_fail(e, "cudaMalloc(batch scratch)"));
   if ((e = cudaMalloc(&p->d_jobs, sizeof(BJob) * njobs)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(jobs)"));
   if ((e = cudaMalloc(&p->d_res, sizeof(BRes) * njobs)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(results)"));
-  if ((e = cudaMalloc(&p->d_counter, 256)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(counter)"));
+  if ((e = cudaMalloc(&p->d_counter, sizeof(unsigned) * (1 + njobs))) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaMalloc(counters)"));
   if ((e = cudaEventCreate(&p->e0)) != cudaSuccess || (e = cudaEventCreate(&p->e1)) != cudaSuccess)
     return bail(cuda_fail(e, "cudaEventCreate"));
 
@@ -385,6 +478,31 @@ int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_
   if ((e = cudaMemcpy(p->d_jobs, table.data(), sizeof(BJob) * njobs, cudaMemcpyHostToDevice)) != cudaSuccess)
     return bail(cuda_fail(e, "cudaMemcpy(jobs)"));
 
+  // work items: stencil jobs above the balancing unit are cut into row slices
+  // (at most one per SM, so every slice of a job can be held at once)
+  double total_cost = 0.0;
+  for (int i = 0; i < njobs; i++) total_cost += cost[i];
+  const double unit = total_cost / (2.0 * dev->sms);
+  std::vector<BItem> items;
+  for (int q = 0; q < njobs; q++) {
+    const perks_job& J = jobs[p->order[q]];
+    int g = 1;
+    if (J.kind == PERKS_JOB_STENCIL && J.steps > 0) {
+      const int rows = J.h * J.wy;
+      g = int(std::min<double>(std::ceil(cost[p->order[q]] / unit), double(std::min(dev->sms, rows))));
+      g = std::max(g, 1);
+    }
+    if (g > 1) p->sliced++;
+    const int rows = J.kind == PERKS_JOB_STENCIL ? J.h * J.wy : 0;
+    for (int sl = 0; sl < g; sl++)
+      items.push_back(BItem{q, sl, g, int((long long)rows * sl / g), int((long long)rows * (sl + 1) / g)});
+  }
+  p->nitems = int(items.size());
+  if ((e = cudaMalloc(&p->d_items, sizeof(BItem) * items.size())) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaMalloc(items)"));
+  if ((e = cudaMemcpy(p->d_items, items.data(), sizeof(BItem) * items.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaMemcpy(items)"));
+
   // launch shape: the caller's, or the fastest candidate of one timed run each
   std::vector<std::pair<int, int>> cand;
   for (int t : {256, 512, 1024})
@@ -392,6 +510,21 @@ int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_
       if ((o.threads == 0 || o.threads == t) && (o.ctas_per_sm == 0 || o.ctas_per_sm == c) && t * c <= 1024)
         cand.push_back({t, c});  // <= 1024 threads per SM: 64 registers per thread fit
   if (cand.empty()) return bail(fail(PERKS_ERR_INVALID_ARG, "threads x ctas_per_sm must be <= 1024"));
+  // every CTA of the grid must be resident (job barriers wait for each other)
+  {
+    std::vector<std::pair<int, int>> fit;
+    for (auto& tc : cand) {
+      int nb = 0;
+      const unsigned sm = smem_for(dev, tc.second);
+      if ((e = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm))) != cudaSuccess)
+        return bail(cuda_fail(e, "cudaFuncSetAttribute(batch)"));
+      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_kernel, tc.first, sm)) != cudaSuccess)
+        return bail(cuda_fail(e, "occupancy(batch)"));
+      if (nb >= tc.second) fit.push_back(tc);
+    }
+    cand.swap(fit);
+    if (cand.empty()) return bail(fail(PERKS_ERR_LAUNCH, "batch launch shape does not fit an SM"));
+  }
   float best = 1e30f;
   if (cand.size() > 1) {  // warm-up (module load, cold L2) before the timed candidates
     float ms = 0.f;
@@ -412,8 +545,12 @@ int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_
   p->smem = smem_for(dev, p->ctas_per_sm);
   p->grid = dev->sms * p->ctas_per_sm;
   p->resident = 0;
-  for (int q = 0; q < njobs; q++)
-    if (p->cells_of[q] > 0 && 2 * p->cells_of[q] <= (long long)p->smem) p->resident++;
+  {
+    std::vector<int> slices(njobs, 1);
+    for (const BItem& it : items) slices[it.job] = it.nslices;
+    for (int q = 0; q < njobs; q++)
+      if (slices[q] == 1 && p->cells_of[q] > 0 && 2 * p->cells_of[q] <= (long long)p->smem) p->resident++;
+  }
 
   // the run as a graph: reset the queue counter, launch
   if ((e = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(p->smem))) != cudaSuccess)
@@ -423,8 +560,9 @@ int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_
     return bail(cuda_fail(e, "cudaStreamCreate"));
   e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned), cs);
-    batch_kernel<<<p->grid, p->threads, p->smem, cs>>>(p->d_jobs, p->njobs, p->d_res, p->d_counter, p->smem);
+    cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned) * (1 + p->njobs), cs);
+    batch_kernel<<<p->grid, p->threads, p->smem, cs>>>(p->d_jobs, p->d_items, p->nitems, p->d_res, p->d_counter,
+                                                       p->smem);
     e = cudaStreamEndCapture(cs, &p->graph);
   }
   cudaStreamDestroy(cs);
@@ -454,6 +592,7 @@ int perks_batch_plan_run(perks_batch_plan p, void* stream, perks_batch_stats* st
     st->grid = p->grid;
     st->resident_jobs = p->resident;
     st->tuned = p->tuned;
+    st->sliced_jobs = p->sliced;
   }
   return PERKS_OK;
 }

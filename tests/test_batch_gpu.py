@@ -29,7 +29,7 @@ def _build(cuda, torch, seed=7):
     # (shape, dims, steps): small ones stay in shared memory, large ones stream
     cases = [("2d5pt", (48, 70), 7), ("2ds9pt", (33, 129), 3), ("2d9pt", (64, 64), 11), ("2d5pt", (300, 257), 5),
              ("2ds9pt", (513, 200), 2), ("2d9pt", (1, 37), 4), ("3d7pt", (20, 30, 17), 6), ("3d7pt", (40, 50, 61), 3),
-             ("3d7pt", (1, 1, 1), 2), ("2d5pt", (96, 96), 0)]
+             ("3d7pt", (1, 1, 1), 2), ("2d5pt", (96, 96), 0), ("2ds9pt", (1100, 700), 9)]
     for k, (shape, dims, steps) in enumerate(cases * 2):
         dt = np.float32 if k % 2 == 0 else np.float64
         f = rng.random(dims).astype(dt)
@@ -63,7 +63,7 @@ def test_batch_matches_oracle(native, cuda, oracle, threads, ctas):
             st = plan.run()
             res = plan.results()
             torch.cuda.synchronize()
-            assert st["resident_jobs"] > 0
+            assert st["resident_jobs"] > 0 and st["sliced_jobs"] > 0
             assert st["tuned"] == (1 if threads == 0 else 0)
             for j, shape, f, steps, o in stencils:
                 assert res[j]["status"] == 0 and res[j]["iterations"] == steps
