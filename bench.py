@@ -365,44 +365,13 @@ def extra_cg(P, torch):
 
 
 def extra_batch(P, torch, n_jobs=512, steps=100, seed=42):
-    """The batched uneven workload: n_jobs instances, a third each of 2D
-    5/9-point stencils (64^2..1024^2, log-uniform), 3D 7-point stencils
-    (32^3..128^3) and CG on 2D/3D Laplacians (n = 1e3..1e5, log-uniform) with a
-    diagonal shift U(0, 0.5); FP32 and FP64 alternating; `steps` time steps per
-    stencil; CG to 1e-10 (FP64) / 1e-5 (FP32). One persistent launch (a CUDA
-    graph, autotuned launch shape) against every instance run alone through
-    the single-instance entry points (sum of their device times)."""
-    import math
-    import numpy as np
-    from perks_gb300 import matrices as M
-    from perks_gb300.batch import BatchPlan, cg_job, stencil_job
-    rng = np.random.default_rng(seed)
-    dev = torch.device("cuda")
-    jobs, alone = [], []
-    for k in range(n_jobs):
-        kind, dt = k % 3, (torch.float32 if (k // 3) % 2 == 0 else torch.float64)
-        if kind < 2:
-            lo, hi = (64, 1024) if kind == 0 else (32, 128)
-            m = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
-            dims = (m, m) if kind == 0 else (m, m, m)
-            shape = ("2d5pt" if rng.random() < 0.5 else "2ds9pt") if kind == 0 else "3d7pt"
-            a = torch.rand(dims, dtype=dt, device=dev)
-            o = torch.empty_like(a)
-            jobs.append(stencil_job(a, o, shape, steps))
-            alone.append(("stencil", a, shape))
-        else:
-            nt = math.exp(rng.uniform(math.log(1e3), math.log(1e5)))
-            if rng.random() < 0.5:
-                rp, ci, v = M.laplacian_2d(max(8, int(round(math.sqrt(nt)))))
-            else:
-                rp, ci, v = M.laplacian_3d(max(4, int(round(nt ** (1 / 3)))))
-            rp, ci, v = M.shifted(rp, ci, v, rng.uniform(0, 0.5))
-            b = rng.uniform(-1, 1, len(rp) - 1)
-            tol = 1e-10 if dt == torch.float64 else 1e-5
-            t = lambda x, ty: torch.from_numpy(np.ascontiguousarray(x)).to(dev, ty)
-            x = torch.empty(len(b), dtype=dt, device=dev)
-            jobs.append(cg_job(t(rp, torch.int32), t(ci, torch.int32), t(v, dt), t(b, dt), x, tol=tol, max_iter=20000))
-            alone.append(("cg", (rp, ci, v, b), "fp64" if dt == torch.float64 else "fp32", tol))
+    """The batched uneven workload (perks_gb300.batch.synthetic_workload: 512
+    instances of 2D/3D stencils and shifted-Laplacian CG, FP32/FP64) in one
+    persistent launch (a CUDA graph, autotuned launch shape), against every
+    instance run alone through the single-instance entry points (sum of their
+    device times)."""
+    from perks_gb300.batch import BatchPlan, synthetic_workload
+    jobs, alone = synthetic_workload(n_jobs, steps, seed)
     with BatchPlan(jobs) as plan:
         plan.run()
         runs = [plan.run() for _ in range(3)]
@@ -423,7 +392,7 @@ def extra_batch(P, torch, n_jobs=512, steps=100, seed=42):
     return {"batch_512": {"jobs": n_jobs, "batch_ms": round(st["ms"], 2), "alone_ms_sum": round(alone_ms, 2),
                           "speedup": round(alone_ms / st["ms"], 2), "threads": st["threads"],
                           "ctas_per_sm": st["ctas_per_sm"], "resident_stencil_jobs": st["resident_jobs"],
-                          "jobs_not_ok": bad}}
+                          "sliced_stencil_jobs": st["sliced_jobs"], "jobs_not_ok": bad}}
 
 
 def kernel_cached_fraction(P, d_in, d_out):

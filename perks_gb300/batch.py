@@ -91,3 +91,50 @@ class BatchPlan:
             self.close()
         except Exception:
             pass
+
+
+def synthetic_workload(n_jobs: int = 512, steps: int = 100, seed: int = 42, device="cuda"):
+    """The batched uneven workload of the benchmark: n_jobs instances, a third
+    each of 2D 5/9-point stencils (64^2..1024^2, log-uniform), 3D 7-point
+    stencils (32^3..128^3) and CG on 2D/3D Laplacians (n = 1e3..1e5,
+    log-uniform) with a diagonal shift U(0, 0.5); FP32 and FP64 alternating;
+    `steps` time steps per stencil; CG to 1e-10 (FP64) / 1e-5 (FP32). Seeded
+    uniform [0,1) fields and uniform [-1,1) right-hand sides.
+
+    Returns (jobs, alone): the batch jobs, and per job what the
+    single-instance path needs: ("stencil", field, shape) or
+    ("cg", (row_ptr, col, val, b), dtype, tol)."""
+    import math
+
+    import numpy as np
+    import torch
+
+    from . import matrices as M
+    rng = np.random.default_rng(seed)
+    gen = torch.Generator(device="cpu").manual_seed(seed)
+    dev = torch.device(device)
+    jobs, alone = [], []
+    for k in range(n_jobs):
+        kind, dt = k % 3, (torch.float32 if (k // 3) % 2 == 0 else torch.float64)
+        if kind < 2:
+            lo, hi = (64, 1024) if kind == 0 else (32, 128)
+            m = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+            dims = (m, m) if kind == 0 else (m, m, m)
+            shape = ("2d5pt" if rng.random() < 0.5 else "2ds9pt") if kind == 0 else "3d7pt"
+            a = torch.rand(dims, generator=gen, dtype=dt).to(dev)
+            jobs.append(stencil_job(a, torch.empty_like(a), shape, steps))
+            alone.append(("stencil", a, shape))
+        else:
+            nt = math.exp(rng.uniform(math.log(1e3), math.log(1e5)))
+            if rng.random() < 0.5:
+                rp, ci, v = M.laplacian_2d(max(8, int(round(math.sqrt(nt)))))
+            else:
+                rp, ci, v = M.laplacian_3d(max(4, int(round(nt ** (1 / 3)))))
+            rp, ci, v = M.shifted(rp, ci, v, rng.uniform(0, 0.5))
+            b = rng.uniform(-1, 1, len(rp) - 1)
+            tol = 1e-10 if dt == torch.float64 else 1e-5
+            t = lambda x, ty: torch.from_numpy(np.ascontiguousarray(x)).to(dev, ty)
+            x = torch.empty(len(b), dtype=dt, device=dev)
+            jobs.append(cg_job(t(rp, torch.int32), t(ci, torch.int32), t(v, dt), t(b, dt), x, tol=tol, max_iter=20000))
+            alone.append(("cg", (rp, ci, v, b), "fp64" if dt == torch.float64 else "fp32", tol))
+    return jobs, alone

@@ -531,14 +531,20 @@ int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_
     int rc = launch_once(p, p->stream, cand[0].first, cand[0].second, smem_for(dev, cand[0].second), &ms);
     if (rc != PERKS_OK) return bail(rc);
   }
-  for (auto& tc : cand) {
-    float ms = 0.f;
-    int rc = launch_once(p, p->stream, tc.first, tc.second, smem_for(dev, tc.second), &ms);
-    if (rc != PERKS_OK) return bail(rc);
-    if (cand.size() == 1 || ms < best) {
-      best = ms;
-      p->threads = tc.first;
-      p->ctas_per_sm = tc.second;
+  if (cand.size() == 1) {  // a fixed launch shape: nothing to time
+    p->threads = cand[0].first;
+    p->ctas_per_sm = cand[0].second;
+    best = 0.f;
+  } else {
+    for (auto& tc : cand) {
+      float ms = 0.f;
+      int rc = launch_once(p, p->stream, tc.first, tc.second, smem_for(dev, tc.second), &ms);
+      if (rc != PERKS_OK) return bail(rc);
+      if (ms < best) {
+        best = ms;
+        p->threads = tc.first;
+        p->ctas_per_sm = tc.second;
+      }
     }
   }
   p->tuned = cand.size() > 1;

@@ -2,12 +2,16 @@
 
   python -m perks_gb300.profile stencil --shape 3d27pt --dims 256,256,256 --dtype f32 --order fast --steps 3
   python -m perks_gb300.profile cg --matrix lap2d --n 512 --dtype fp64 --iters 20
+  python -m perks_gb300.profile batch --jobs 512 --steps 100
 
 Runs one warm-up call, then exactly one call of the requested size, and
 prints its stats as one JSON line. The warm-up uses the same kernel with 2
 time steps (stencil) or 2 iterations (CG), so an ncu filter of
 `-k regex:<kernel> -s 1 -c 1` captures the second call. Fields are seeded
-uniform [0,1); CG right-hand sides uniform [-1,1).
+uniform [0,1); CG right-hand sides uniform [-1,1). `batch` builds the
+benchmark's batched workload and runs it once with a fixed launch shape (the
+autotuner's candidate runs would be captured otherwise): the only
+batch_kernel launch, `-k regex:batch_kernel -c 1`.
 """
 from __future__ import annotations
 
@@ -50,6 +54,17 @@ def _cg(a):
     return {"matrix": a.matrix, "n": a.n, "format": a.format, "dtype": a.dtype, **res}
 
 
+def _batch(a):
+    import torch
+    from .batch import BatchPlan, synthetic_workload
+    jobs, _ = synthetic_workload(a.jobs, a.steps, a.seed)
+    with BatchPlan(jobs, threads=a.threads, ctas_per_sm=a.ctas) as plan:
+        st = plan.run()
+        bad = sum(1 for r in plan.results() if r["status"] != 0)
+    torch.cuda.synchronize()
+    return {"jobs": a.jobs, "steps": a.steps, "jobs_not_ok": bad, **st}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m perks_gb300.profile")
     sub = ap.add_subparsers(dest="what", required=True)
@@ -67,8 +82,14 @@ def main(argv=None):
     c.add_argument("--format", default="csr", choices=["csr", "dia"])
     c.add_argument("--dtype", default="fp64", choices=["fp64", "fp32", "mixed"])
     c.add_argument("--iters", type=int, default=20)
+    bt = sub.add_parser("batch")
+    bt.add_argument("--jobs", type=int, default=512)
+    bt.add_argument("--steps", type=int, default=100)
+    bt.add_argument("--seed", type=int, default=42)
+    bt.add_argument("--threads", type=int, default=1024, help="threads per CTA (0 = autotune)")
+    bt.add_argument("--ctas", type=int, default=1, help="CTAs per SM (0 = autotune)")
     a = ap.parse_args(argv)
-    out = _stencil(a) if a.what == "stencil" else _cg(a)
+    out = {"stencil": _stencil, "cg": _cg, "batch": _batch}[a.what](a)
     print(json.dumps(out, default=str), flush=True)
 
 
