@@ -61,7 +61,11 @@ struct Cfg2D {
   // (box shapes also hold the double-precision partial sums of the reference order)
   static constexpr int REG_EST =
       int(sizeof(T) / 4) * (BOX ? WN * (V + 2 * H) + V : WN * (V + 1) + (V + 2 * H) + V) + (BOX ? 72 : 40);
-  static constexpr int NW = (REG_EST <= 64 && !BOX) ? 32 : REG_EST <= 80 ? 24 : REG_EST <= 110 ? 16 : 8;
+  static constexpr int NW_REG = (REG_EST <= 64 && !BOX) ? 32 : REG_EST <= 80 ? 24 : REG_EST <= 110 ? 16 : 8;
+  // FP32 star shapes of radius 2 and 3: 12 warps (168 registers per thread)
+  // measured faster than 16 (128 registers) and 8 on GB300 (2ds9pt 686 vs 662
+  // GCells/s, 2d13pt 487 vs 416, reference order, 8192^2)
+  static constexpr int NW = (sizeof(T) == 4 && !BOX && (H == 2 || H == 3)) ? 12 : NW_REG;
   static constexpr int NT = NW * 32;
   static constexpr int D = NW >= 24 ? 3 : NW == 16 ? 4 : 6;  // rows in flight per warp
   static constexpr int DR = D + 1;                       // ring slots per warp
