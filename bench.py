@@ -36,10 +36,10 @@ METRIC = "GCells/s per stencil & CG time-to-1e-10 rel. residual; mixed vs FP64 o
 UNIT = "GCells/s"
 # DRAM bytes (read + write) per cell per time step of the persistent kernel:
 # dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of a 20-step
-# launch on the same field (10.146 GB / (20 x 8192^2)), see
+# launch on the same field (10.102 GB / (20 x 8192^2)), see
 # profiles/stencil2d_2ds9pt_f32_8192.txt. The per-step traffic does not depend
 # on the number of steps, so a 1000-step launch moves 1000 times as much.
-TRAFFIC_PER_CELL_STEP = 7.56
+TRAFFIC_PER_CELL_STEP = 7.53
 
 
 def measured_hbm_peak():
