@@ -19,6 +19,10 @@
 // of 2g and b/2 is odd), so the test needs no magnitude check. The quotient
 // takes the sign of x, which fixes the sign of zero results.
 //
+// For even b with b*RN(1/b) > 1 (b = 118 in float) the midpoint fix needs no
+// second candidate: the fma then always lands on the neighbour away from q0,
+// which is kept when its last bit is even and replaced by q0 otherwise.
+//
 // The float version is checked against IEEE division for all 2^32 inputs
 // with b = 118 and b = 159 (zero mismatches), the double version through the
 // bit-exact stencil tests on subnormal, tiny, huge, infinite and NaN fields.
@@ -36,8 +40,15 @@ __device__ __forceinline__ float div_finish(float x, float q0, float e, float q1
   if constexpr ((B & 1) == 0) {
     constexpr float half = float(B / 2) * 0x1p-149f;  // b/2 subnormal steps
     const bool tie = fabsf(e) == half;
-    const float up = __fadd_rn(q0, copysignf(0x1p-149f, e));
-    q1 = tie ? ((__float_as_uint(q0) & 1u) ? up : q0) : q1;
+    // At a midpoint e*r = +-(g/2)(b*r) exactly, so with b*RN(1/b) > 1 the fma
+    // lands on the neighbour away from q0: keep it if even, else take q0.
+    constexpr bool far_on_tie = double(B) * double(1.0f / float(B)) > 1.0;
+    if constexpr (far_on_tie) {
+      q1 = (tie && (__float_as_uint(q1) & 1u)) ? q0 : q1;
+    } else {
+      const float up = __fadd_rn(q0, copysignf(0x1p-149f, e));
+      q1 = tie ? ((__float_as_uint(q0) & 1u) ? up : q0) : q1;
+    }
   }
   return isfinite(q0) ? copysignf(q1, x) : q0;
 }
