@@ -279,6 +279,19 @@ PERKS_API int perks_batch_plan_run(perks_batch_plan plan, void* stream, perks_ba
 PERKS_API int perks_batch_plan_results(perks_batch_plan plan, perks_job_result* results);
 PERKS_API void perks_batch_plan_destroy(perks_batch_plan plan);
 
+/* ------------------------------------------------------------ MatrixMarket */
+/* Host code (no GPU). Reads a MatrixMarket file as the reference's
+ * CooMatrix::InitMarket + CsrMatrix::Init do
+ * (conjugateGradient/matrix/sparse_matrix.h:217-380, 633-730): coordinate
+ * real/integer/pattern (a missing value reads as 1.0) or array files,
+ * symmetric and skew-symmetric files with every off-diagonal entry mirrored,
+ * entries stably sorted by (row, column), duplicates kept. perks_mtx_size
+ * gives the dimensions and the entry count after mirroring; perks_mtx_read_csr
+ * fills caller arrays row_ptr[rows+1], col[nnz], val[nnz]. */
+PERKS_API int perks_mtx_size(const char* path, int* rows, int* cols, long long* nnz);
+PERKS_API int perks_mtx_read_csr(const char* path, int rows, long long nnz_cap, int* row_ptr, int* col,
+                                 double* val, long long* nnz);
+
 /* ------------------------------------------------------------------ misc */
 PERKS_API const char* perks_last_error(void);     /* thread-local message of the last failure */
 PERKS_API const char* perks_status_string(int status);

@@ -105,6 +105,10 @@ SIGNATURES = {
     "perks_batch_plan_run": (c_int, [c_void_p, c_void_p, ctypes.POINTER(BatchStats)]),
     "perks_batch_plan_results": (c_int, [c_void_p, ctypes.POINTER(JobResult)]),
     "perks_batch_plan_destroy": (None, [c_void_p]),
+    "perks_mtx_size": (c_int, [ctypes.c_char_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                               ctypes.POINTER(ctypes.c_longlong)]),
+    "perks_mtx_read_csr": (c_int, [ctypes.c_char_p, c_int, ctypes.c_longlong, c_void_p, c_void_p, c_void_p,
+                                   ctypes.POINTER(ctypes.c_longlong)]),
     "perks_last_error": (ctypes.c_char_p, []),
     "perks_status_string": (ctypes.c_char_p, [c_int]),
     "perks_abi_version": (c_int, []),

@@ -133,3 +133,24 @@ def shifted(row_ptr, col, val, shift: float):
     v = val.copy()
     v[rows == col] += shift
     return row_ptr, col, v
+
+
+def read_mtx(path: str):
+    """A MatrixMarket file as CSR (row_ptr int32, col int32, val float64),
+    read by the library the way the reference's CooMatrix::InitMarket and
+    CsrMatrix::Init read it (symmetric entries mirrored, rows and columns
+    sorted, duplicates kept, pattern values 1.0). Host only."""
+    import ctypes
+
+    from . import _native as N
+    L = N.lib()
+    rows, cols, nnz = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+    b = str(path).encode()
+    N.check(L.perks_mtx_size(b, ctypes.byref(rows), ctypes.byref(cols), ctypes.byref(nnz)))
+    rp = np.zeros(rows.value + 1, np.int32)
+    ci = np.zeros(max(nnz.value, 1), np.int32)
+    val = np.zeros(max(nnz.value, 1), np.float64)
+    got = ctypes.c_longlong()
+    N.check(L.perks_mtx_read_csr(b, rows.value, nnz.value, rp.ctypes.data, ci.ctypes.data, val.ctypes.data,
+                                 ctypes.byref(got)))
+    return rp, ci[:got.value], val[:got.value]
