@@ -36,7 +36,7 @@ METRIC = "GCells/s per stencil & CG time-to-1e-10 rel. residual; mixed vs FP64 o
 UNIT = "GCells/s"
 # DRAM bytes (read + write) per cell per time step of the persistent kernel:
 # dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of a 20-step
-# launch on the same field (10.102 GB / (20 x 8192^2)), see
+# launch on the same field (10.101 GB / (20 x 8192^2)), see
 # profiles/stencil2d_2ds9pt_f32_8192.txt. The per-step traffic does not depend
 # on the number of steps, so a 1000-step launch moves 1000 times as much.
 TRAFFIC_PER_CELL_STEP = 7.53
@@ -297,6 +297,7 @@ def main():
         extra["persistent_fast_fp64_gcells"] = round(st["gcells_per_s"], 2)
         del d64, o64
         extra["cached_fraction"] = round(kernel_cached_fraction(P, d_in, d_out), 4)
+        extra.update(extra_min_domain(P, torch))
         extra.update(extra_3d(P, torch))
         extra.update(extra_cg(P, torch))
         extra.update(extra_batch(P, torch))
@@ -325,6 +326,28 @@ def main():
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def extra_min_domain(P, torch, steps=1000):
+    """All-on-chip throughput: the headline shape at the largest 8192-wide
+    field whose rows the persistent kernel keeps in shared memory (the
+    reference's --small mode), against one launch per step at that size."""
+    import numpy as np
+    out = {}
+    for dt, tag in ((torch.float32, "fp32"), (torch.float64, "fp64")):
+        wy = P.min_domain_2d(SHAPE, WX, dtype=np.float64 if dt == torch.float64 else np.float32)
+        d = torch.rand((wy, WX), dtype=dt, device="cuda")
+        o = torch.empty_like(d)
+        n = steps if tag == "fp32" else steps // 10
+        P.stencil2d(d, SHAPE, 3, out=o)
+        _, st = P.stencil2d(d, SHAPE, n, out=o)
+        _, st1 = P.stencil2d(d, SHAPE, n, out=o, kernel="per_step")
+        out[f"min_domain_{tag}"] = {"width_y": wy, "width_x": WX, "steps": n,
+                                    "cached_fraction": round(st["cached_fraction"], 4),
+                                    "persistent_gcells": round(st["gcells_per_s"], 2),
+                                    "per_step_gcells": round(st1["gcells_per_s"], 2)}
+        del d, o
+    return out
 
 
 def extra_3d(P, torch):

@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define PERKS_ABI_VERSION 1
+#define PERKS_ABI_VERSION 2
 
 /* ------------------------------------------------------------------ codes */
 typedef enum {
@@ -148,7 +148,11 @@ PERKS_API int perks_jacobi_iterative_f64(int shape, const double* h_in, int widt
                                double* h_out, int bdimx, int blkpsm, int iteration, int async,
                                int useSM, int usewarmup, int warmupiteration, int isDoubleTile);
 /* Replaces j3d_iterative<float/double> (stencil/3dstencil/common/jacobi_cuda.cuh:6-10).
- * Reference return codes kept: -2 unsupported widths, -4 height too small. */
+ * Reference return codes kept: -2 unsupported widths, -4 height too small.
+ * getminHeight=1 returns the minimum-domain height without running (h_in and
+ * h_out may be NULL); it is 0, the reference's answer for a kernel without a
+ * plane cache (j3d.driver.cpp:102-108), because the 3D kernel streams every
+ * plane through its TMA ring each step and keeps none on chip. */
 PERKS_API int perks_j3d_iterative_f32(int shape, const float* h_in, int height, int width_y, int width_x,
                             float* h_out, int bdimx, int blkpsm, int iteration, int useSM,
                             int usewarmup, int warmupiteration, int isDoubleTile, int getminHeight);
@@ -156,11 +160,42 @@ PERKS_API int perks_j3d_iterative_f64(int shape, const double* h_in, int height,
                             double* h_out, int bdimx, int blkpsm, int iteration, int useSM,
                             int usewarmup, int warmupiteration, int isDoubleTile, int getminHeight);
 
+/* Minimum-domain mode (the reference's --small: jacobi.driver.cpp:84-109
+ * with getMinWidthY, stencil/2dstencil/jacobi-2d.cu:79-136). Writes to
+ * *width_y the largest height of a width_x-wide field at which the persistent
+ * 2D kernel keeps, between time steps, every row in shared memory except the
+ * H rows at each end of each row band (those are the halo the neighbouring
+ * bands read from the field). Depends on shape, dtype, cache_rows and ctas of
+ * `opts`; 0 when the options cache nothing (per-step kernel, cache_rows=0). */
+PERKS_API int perks_stencil2d_min_domain(const perks_stencil_opts* opts, int width_x, int* width_y);
+/* getMinWidthY<REAL>(width_x, bdimx, registers, useSM, blkpsm, isDoubleTile)
+ * (stencil/2dstencil/common/jacobi_cuda.cuh:14) with the shape and dtype
+ * first: returns that width_y (>= 0) or a negative perks_status. bdimx,
+ * registers, blkpsm and isDoubleTile are accepted and ignored. */
+PERKS_API int perks_get_min_width_y(int shape, int dtype, int width_x, int bdimx, int registers, int useSM,
+                                    int blkpsm, int isDoubleTile);
+
 /* --------------------------------------------------------------------- CG */
 typedef enum {
   PERKS_STOP_ABS_RR = 0, /* reference: stop when r.r < tol*tol (cg_kernels.cuh:834) */
   PERKS_STOP_REL = 1     /* stop when ||r|| / ||b|| < tol */
 } perks_cg_stop;
+
+/* CG checkpoint: the iteration state between two iterations, so that a
+ * solve can stop and later resume exactly where it stopped (the resumed run
+ * gives bit-identical x and r to one uninterrupted run with the same options).
+ * The caller owns d_r and d_p (n elements of the working type: FP64 for
+ * PERKS_FP64, FP32 for PERKS_FP32); the solution itself is the caller's x.
+ * Not available for PERKS_MIXED. */
+typedef struct {
+  void* d_r;        /* device: residual r */
+  void* d_p;        /* device: the last search direction p */
+  double rr;        /* r.r as the iteration holds it (in the working precision) */
+  double rr_prev;   /* r.r one iteration earlier (for beta) */
+  double bb;        /* b.b (relative stop) */
+  int k;            /* iterations completed; 0 = no state yet (start from x) */
+  int kernel;       /* perks_kernel that wrote the state; resuming needs the same */
+} perks_cg_state;
 
 typedef struct {
   int dtype;          /* PERKS_FP64, PERKS_FP32 (reference float build), PERKS_MIXED
@@ -174,6 +209,11 @@ typedef struct {
                          (0 = auto) */
   int ctas;           /* CTAs in the persistent grid; 0 = auto */
   void* stream;       /* cudaStream_t */
+  perks_cg_state* checkpoint; /* NULL = none. Otherwise the solve resumes from *checkpoint when
+                                 checkpoint->k > 0 (x must hold the iterate saved with it) and
+                                 writes its final state back, also when it returns
+                                 PERKS_ERR_NOT_CONVERGED. max_iter counts all iterations,
+                                 including those before the checkpoint. */
 } perks_cg_opts;
 
 typedef struct {

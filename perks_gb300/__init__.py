@@ -6,8 +6,9 @@ this package is its ctypes host mirror.
 """
 from . import _native
 from ._native import PerksError, SHAPES, HALO, lib
-from .stencil import j3d_iterative, jacobi_iterative, last_error, stencil2d, stencil3d
-from .cg import cg_csr, cg_dia, spmv_csr, spmv_dia
+from .stencil import (getMinWidthY, j3d_iterative, jacobi_iterative, last_error, min_domain_2d, stencil2d,
+                      stencil3d)
+from .cg import CgCheckpoint, cg_csr, cg_dia, spmv_csr, spmv_dia
 from .batch import BatchPlan, cg_job, stencil_job
 
 __all__ = ["PerksError", "SHAPES", "HALO", "lib", "jacobi_iterative", "j3d_iterative", "stencil2d",

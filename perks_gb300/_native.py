@@ -45,10 +45,15 @@ class StencilStats(ctypes.Structure):
                 ("tile_y", c_int), ("cached_rows", c_int), ("launches", c_int)]
 
 
+class CgState(ctypes.Structure):
+    _fields_ = [("d_r", c_void_p), ("d_p", c_void_p), ("rr", c_double), ("rr_prev", c_double),
+                ("bb", c_double), ("k", c_int), ("kernel", c_int)]
+
+
 class CgOpts(ctypes.Structure):
     _fields_ = [("dtype", c_int), ("stop", c_int), ("tol", c_double), ("max_iter", c_int),
                 ("static_iter", c_int), ("kernel", c_int), ("replace_every", c_int), ("ctas", c_int),
-                ("stream", c_void_p)]
+                ("stream", c_void_p), ("checkpoint", ctypes.POINTER(CgState))]
 
 
 class CgResult(ctypes.Structure):
@@ -87,6 +92,8 @@ SIGNATURES = {
                                 ctypes.POINTER(StencilStats)]),
     "perks_stencil2d_noalloc": (c_int, [ctypes.POINTER(StencilOpts), c_void_p, c_void_p, c_int, c_int, c_int,
                                         ctypes.POINTER(StencilStats)]),
+    "perks_stencil2d_min_domain": (c_int, [ctypes.POINTER(StencilOpts), c_int, ctypes.POINTER(c_int)]),
+    "perks_get_min_width_y": (c_int, [c_int] * 8),
     "perks_jacobi_iterative_f32": (c_int, [c_int, c_void_p, c_int, c_int, c_void_p] + [c_int] * 8),
     "perks_jacobi_iterative_f64": (c_int, [c_int, c_void_p, c_int, c_int, c_void_p] + [c_int] * 8),
     "perks_j3d_iterative_f32": (c_int, [c_int, c_void_p, c_int, c_int, c_int, c_void_p] + [c_int] * 8),
@@ -117,6 +124,7 @@ SIGNATURES = {
 }
 
 _lib = None
+ABI_VERSION = 2  # PERKS_ABI_VERSION of include/perks.h that the structures above follow
 
 
 class PerksError(RuntimeError):
@@ -133,6 +141,10 @@ def lib() -> ctypes.CDLL:
             from . import build as _b
             _b.build()
         L = ctypes.CDLL(LIB_PATH)
+        L.perks_abi_version.restype = c_int
+        if L.perks_abi_version() != ABI_VERSION:
+            raise ImportError(f"{LIB_PATH} has ABI version {L.perks_abi_version()}, these bindings need "
+                              f"{ABI_VERSION}: rebuild it (perks_gb300.build.build())")
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(L, name)
             fn.restype = res

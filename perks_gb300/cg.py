@@ -24,6 +24,52 @@ def _dev(a, dtype, device):
     return torch.from_numpy(np.ascontiguousarray(a)).to(device=device, dtype=dtype)
 
 
+class CgCheckpoint:
+    """CG iteration state between two iterations (perks_cg_state): residual r,
+    last search direction p, r.r of the last two iterations, b.b and the
+    iteration count. Pass it as ``checkpoint=`` to cg_csr / cg_dia: a solve
+    resumes from it when it holds a state (k > 0; x0 must then be the
+    iterate saved with it) and leaves its final state in it. ``to_host`` /
+    ``from_host`` move it to numpy (for example to np.savez it with x)."""
+
+    def __init__(self):
+        self.r = None
+        self.p = None
+        self.state = N.CgState()
+
+    @property
+    def k(self) -> int:
+        return self.state.k
+
+    def _bind(self, n, dtype, device):
+        import torch
+        if self.r is None:
+            self.r = torch.zeros(n, dtype=dtype, device=device)
+            self.p = torch.zeros(n, dtype=dtype, device=device)
+        if self.r.numel() != n or self.r.dtype != dtype:
+            raise ValueError("checkpoint holds a state of another size or dtype")
+        self.state.d_r = self.r.data_ptr()
+        self.state.d_p = self.p.data_ptr()
+        return ctypes.pointer(self.state)
+
+    def to_host(self) -> dict:
+        st = self.state
+        return {"r": self.r.cpu().numpy(), "p": self.p.cpu().numpy(), "rr": st.rr, "rr_prev": st.rr_prev,
+                "bb": st.bb, "k": st.k, "kernel": st.kernel}
+
+    @classmethod
+    def from_host(cls, d: dict, device="cuda") -> "CgCheckpoint":
+        import torch
+        c = cls()
+        c.r = torch.from_numpy(np.ascontiguousarray(d["r"])).to(device)
+        c.p = torch.from_numpy(np.ascontiguousarray(d["p"])).to(device)
+        for f in ("rr", "rr_prev", "bb"):
+            setattr(c.state, f, float(d[f]))
+        c.state.k = int(d["k"])
+        c.state.kernel = int(d["kernel"])
+        return c
+
+
 def _opts(dtype="fp64", stop="rel", tol=1e-10, max_iter=100000, static_iter=False, kernel="persistent",
           replace_every=0, ctas=0, stream=None):
     o = N.CgOpts()
@@ -44,9 +90,10 @@ def _result(r: N.CgResult) -> dict:
     return {k: getattr(r, k) for k, _ in N.CgResult._fields_}
 
 
-def cg_csr(row_ptr, col, val, b, x0=None, *, dtype="fp64", device="cuda", check=True, **kw):
+def cg_csr(row_ptr, col, val, b, x0=None, *, dtype="fp64", device="cuda", check=True, checkpoint=None, **kw):
     """Solve with CSR A. dtype: 'fp64', 'fp32' (the reference's float build)
-    or 'mixed' (FP32 inner CG, FP64 solution/residual). Returns (x, result)."""
+    or 'mixed' (FP32 inner CG, FP64 solution/residual). `checkpoint`: a
+    CgCheckpoint to resume from and to save into. Returns (x, result)."""
     import torch
     vdt = torch.float32 if dtype == "fp32" else torch.float64
     rp = _dev(row_ptr, torch.int32, device)
@@ -58,6 +105,8 @@ def cg_csr(row_ptr, col, val, b, x0=None, *, dtype="fp64", device="cuda", check=
     if "stream" not in kw:
         kw["stream"] = ctypes.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
     o = _opts(dtype, **kw)
+    if checkpoint is not None:
+        o.checkpoint = checkpoint._bind(n, vdt, x.device)
     res = N.CgResult()
     rc = N.lib().perks_cg_csr(n, ci.numel(), rp.data_ptr(), ci.data_ptr(), v.data_ptr(), bb.data_ptr(),
                               x.data_ptr(), ctypes.byref(o), ctypes.byref(res))
@@ -68,7 +117,7 @@ def cg_csr(row_ptr, col, val, b, x0=None, *, dtype="fp64", device="cuda", check=
     return x, out
 
 
-def cg_dia(offsets, data, b, x0=None, *, dtype="fp64", device="cuda", check=True, **kw):
+def cg_dia(offsets, data, b, x0=None, *, dtype="fp64", device="cuda", check=True, checkpoint=None, **kw):
     """Solve with DIA A (offsets[ndiag], data[ndiag][n], diagonal-major)."""
     import torch
     vdt = torch.float32 if dtype == "fp32" else torch.float64
@@ -80,6 +129,8 @@ def cg_dia(offsets, data, b, x0=None, *, dtype="fp64", device="cuda", check=True
     if "stream" not in kw:
         kw["stream"] = ctypes.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
     o = _opts(dtype, **kw)
+    if checkpoint is not None:
+        o.checkpoint = checkpoint._bind(n, vdt, x.device)
     res = N.CgResult()
     rc = N.lib().perks_cg_dia(n, len(off), off.ctypes.data, d.data_ptr(), bb.data_ptr(), x.data_ptr(),
                               ctypes.byref(o), ctypes.byref(res))

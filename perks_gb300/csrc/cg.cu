@@ -80,7 +80,10 @@ struct CgParams {
   double delta2;          // reliable-update threshold (squared)
   int* out_iter;          // iterations done
   int* out_outer;         // reliable updates done
-  double* out_rr;         // final r.r
+  double* out_rr;         // final r.r, then r.r one iteration earlier, then b.b
+  // resume from a checkpoint: r and p already in place, scalars here
+  int resume, k0;         // k0 = iterations completed before this launch
+  double rr0, rrp0, bb0;
   unsigned* bar;
   unsigned* status;
 };
@@ -380,23 +383,34 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
   const bool xvec = aligned16(x);  // the caller's solution vector
   const bool v4 = A.fmt != 0 && (A.n & 3) == 0 && aligned16(val) && aligned16(A.eci);  // DIA/ELL columns 16-byte aligned
 
-  // r = b - A x ; rr = r.r ; bb = b.b  (per-thread sums in T, then double)
-  T rr_t = T(0), bb_t = T(0);
-  CG_ROWS(i, {
-    const T ax = spmv_row<FMT>(A, val, x, i);
-    const T bi = b[i];
-    const T ri = T(-1) * ax + bi;
-    r[i] = ri;
-    rr_t = fma(ri, ri, rr_t);
-    bb_t = fma(bi, bi, bb_t);
-  })
-  double rr = double(rr_t), bb = double(bb_t);
-  if (!gs.sum2(0, rr, bb)) return;
-  T r1 = T(rr);  // float build: r.r rounded to float (cg_cpu.cpp:52)
-  T r0 = T(0);
+  T r1, r0;
+  double bb;
+  int k;
+  if (P.resume) {  // r and the last p were restored by the host
+    r1 = T(P.rr0);
+    r0 = T(P.rrp0);
+    bb = P.bb0;
+    k = P.k0 + 1;
+  } else {
+    // r = b - A x ; rr = r.r ; bb = b.b  (per-thread sums in T, then double)
+    T rr_t = T(0), bb_t = T(0);
+    CG_ROWS(i, {
+      const T ax = spmv_row<FMT>(A, val, x, i);
+      const T bi = b[i];
+      const T ri = T(-1) * ax + bi;
+      r[i] = ri;
+      rr_t = fma(ri, ri, rr_t);
+      bb_t = fma(bi, bi, bb_t);
+    })
+    double rr = double(rr_t);
+    bb = double(bb_t);
+    if (!gs.sum2(0, rr, bb)) return;
+    r1 = T(rr);  // float build: r.r rounded to float (cg_cpu.cpp:52)
+    r0 = T(0);
+    k = 1;
+  }
   const double tol2 = (P.stop == PERKS_STOP_REL) ? P.tol * P.tol * bb : P.tol * P.tol;
   const T tol2t = T(P.tol) * T(P.tol);
-  int k = 1;
   while (true) {
     if (!P.static_iter) {
       const bool done = (P.stop == PERKS_STOP_REL) ? (double(r1) < tol2) : (r1 < tol2t);
@@ -528,7 +542,9 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
   }
   if (blockIdx.x == 0 && tid == 0) {
     *P.out_iter = k - 1;
-    *P.out_rr = double(r1);
+    P.out_rr[0] = double(r1);
+    P.out_rr[1] = double(r0);
+    P.out_rr[2] = bb;
     *P.out_outer = 0;
   }
 }
@@ -913,6 +929,14 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
     return fail(PERKS_ERR_INVALID_ARG, "unknown kernel kind");
   if (o->dtype == PERKS_MIXED && o->kernel != PERKS_KERNEL_PERSISTENT)
     return fail(PERKS_ERR_UNSUPPORTED, "mixed precision runs in the persistent kernel only");
+  perks_cg_state* ck = o->checkpoint;
+  if (ck) {
+    if (o->dtype == PERKS_MIXED) return fail(PERKS_ERR_UNSUPPORTED, "no checkpoint for mixed precision");
+    if (!ck->d_r || !ck->d_p || ck->k < 0) return fail(PERKS_ERR_INVALID_ARG, "bad checkpoint");
+    if (ck->k > 0 && ck->kernel != o->kernel)
+      return fail(PERKS_ERR_INVALID_ARG, "checkpoint was written by the other kernel kind");
+  }
+  const bool resume = ck && ck->k > 0;
   const DeviceInfo* dev = device_info();
   if (!dev) return PERKS_ERR_NO_DEVICE;
   cudaStream_t s = static_cast<cudaStream_t>(o->stream);
@@ -956,7 +980,14 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   P.delta2 = 0.1 * 0.1;
   P.out_iter = reinterpret_cast<int*>(scal + 16);
   P.out_outer = reinterpret_cast<int*>(scal + 17);
-  P.out_rr = scal + 18;
+  P.out_rr = scal + 18;  // [18..20]
+  if (resume) {
+    P.resume = 1;
+    P.k0 = ck->k;
+    P.rr0 = ck->rr;
+    P.rrp0 = ck->rr_prev;
+    P.bb0 = ck->bb;
+  }
   P.bar = sw.bar;
   P.status = sw.status;
   PERKS_CUDA(cudaMemsetAsync(scal, 0, 32 * sizeof(double), s));
@@ -1053,6 +1084,13 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
     count_launch(1);
   }
 
+  // the iterate's p: FP32 persistent iterations alternate two buffers
+  // (iteration k writes P.p[k & 1]); the others keep p in P.p[0]
+  auto p_of = [&](int k) { return (f32 && o->kernel == PERKS_KERNEL_PERSISTENT) ? P.p[k & 1] : P.p[0]; };
+  if (resume) {
+    PERKS_CUDA(cudaMemcpyAsync(P.r, ck->d_r, size_t(n) * ws, cudaMemcpyDeviceToDevice, s));
+    PERKS_CUDA(cudaMemcpyAsync(p_of(ck->k), ck->d_p, size_t(n) * ws, cudaMemcpyDeviceToDevice, s));
+  }
   int launches = 0;
   if (o->kernel == PERKS_KERNEL_PERSISTENT) {
     const int f = P.A.fmt;
@@ -1078,16 +1116,25 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
     double* sv = scal;  // s[0..5]
     const int grid = dev->sms * 2, bt = 512;
     double* part = P.part;
-    if (f32) {
+    double flag = 0.0;
+    if (resume) {  // scalars of the checkpoint, with the stop test of cg_phase_reduce
+      const double tol2 = o->stop == PERKS_STOP_REL ? o->tol * o->tol * ck->bb
+                          : f32 ? double(float(o->tol) * float(o->tol)) : o->tol * o->tol;
+      const double hs0[6] = {ck->rr, ck->rr_prev, 0.0, ck->bb,
+                             ((!o->static_iter && ck->rr < tol2) || ck->k >= o->max_iter) ? 1.0 : 0.0,
+                             double(ck->k)};
+      PERKS_CUDA(cudaMemcpyAsync(sv, hs0, sizeof(hs0), cudaMemcpyHostToDevice, s));
+      flag = hs0[4];
+    } else if (f32) {
       cg_phase_init<float><<<grid, bt, 0, s>>>(P, part);
       cg_phase_reduce<float><<<1, 1024, 0, s>>>(P, part, grid, sv, 0);
+      launches = 2;
     } else {
       cg_phase_init<double><<<grid, bt, 0, s>>>(P, part);
       cg_phase_reduce<double><<<1, 1024, 0, s>>>(P, part, grid, sv, 0);
+      launches = 2;
     }
-    launches = 2;
     const int chunk = 32;
-    double flag = 0.0;
     for (int it = 0; it < o->max_iter + 1 && flag == 0.0; it += chunk) {
       for (int c = 0; c < chunk; c++) {
         if (f32) {
@@ -1123,14 +1170,27 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   PERKS_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, s));
   PERKS_CUDA(cudaStreamSynchronize(s));
   int iters = 0, outer = 0;
-  double rr = 0.0;
+  double rr = 0.0, rr_prev = 0.0, bbs = 0.0;
   if (o->kernel == PERKS_KERNEL_PERSISTENT) {
     std::memcpy(&iters, &hs[16], sizeof(int));
     std::memcpy(&outer, &hs[17], sizeof(int));
     rr = hs[18];
+    rr_prev = hs[19];
+    bbs = hs[20];
   } else {
     iters = int(hs[5]);
     rr = hs[0];
+    rr_prev = hs[1];
+    bbs = hs[3];
+  }
+  if (ck) {  // state for a later resume
+    PERKS_CUDA(cudaMemcpyAsync(ck->d_r, P.r, size_t(n) * ws, cudaMemcpyDeviceToDevice, s));
+    PERKS_CUDA(cudaMemcpyAsync(ck->d_p, p_of(iters), size_t(n) * ws, cudaMemcpyDeviceToDevice, s));
+    ck->rr = rr;
+    ck->rr_prev = rr_prev;
+    ck->bb = bbs;
+    ck->k = iters;
+    ck->kernel = o->kernel;
   }
   // true relative residual in FP64
   double* tpart = P.part;
@@ -1138,10 +1198,10 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   const bool val_f32 = f32;
   if (val_f32) cg_true_residual<float><<<tg, 512, 0, s>>>(A, b, x, tpart);
   else cg_true_residual<double><<<tg, 512, 0, s>>>(A, b, x, tpart);
-  sum_partials<<<1, 1024, 0, s>>>(tpart, tg, scal + 20);
+  sum_partials<<<1, 1024, 0, s>>>(tpart, tg, scal + 22);
   count_launch(2);
   double tr[2];
-  PERKS_CUDA(cudaMemcpyAsync(tr, scal + 20, sizeof(tr), cudaMemcpyDeviceToHost, s));
+  PERKS_CUDA(cudaMemcpyAsync(tr, scal + 22, sizeof(tr), cudaMemcpyDeviceToHost, s));
   PERKS_CUDA(cudaStreamSynchronize(s));
   if (res) {
     res->iterations = iters;
@@ -1176,6 +1236,7 @@ void perks_cg_default_opts(perks_cg_opts* o) {
   o->replace_every = 0;
   o->ctas = 0;
   o->stream = nullptr;
+  o->checkpoint = nullptr;
 }
 
 int perks_cg_csr(int n, int nnz, const int* rp, const int* ci, const void* val, const void* b, void* x,

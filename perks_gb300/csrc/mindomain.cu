@@ -1,0 +1,54 @@
+// Minimum-domain queries: the reference's --small mode
+// (stencil/2dstencil/jacobi.driver.cpp:84-109 calls getMinWidthY,
+// stencil/2dstencil/jacobi-2d.cu:79-136, and runs the stencil at the width_y
+// it returns). The answer is the largest domain that the persistent kernel
+// keeps on chip between time steps, used to report all-on-chip throughput.
+// Host arithmetic only; it reads the device's SM count and shared memory.
+#include <string>
+#include "stencil2d_host.cuh"
+
+namespace perks {
+
+template <class T>
+static int min_domain_2d(int shape, const perks_stencil_opts& o, int wx, int* wy) {
+  switch (shape) {
+    case PERKS_2D5PT: return min_domain_rows<T, PERKS_2D5PT>(o, wx, wy);
+    case PERKS_2DS9PT: return min_domain_rows<T, PERKS_2DS9PT>(o, wx, wy);
+    case PERKS_2D13PT: return min_domain_rows<T, PERKS_2D13PT>(o, wx, wy);
+    case PERKS_2D17PT: return min_domain_rows<T, PERKS_2D17PT>(o, wx, wy);
+    case PERKS_2D21PT: return min_domain_rows<T, PERKS_2D21PT>(o, wx, wy);
+    case PERKS_2DS25PT: return min_domain_rows<T, PERKS_2DS25PT>(o, wx, wy);
+    case PERKS_2D9PT: return min_domain_rows<T, PERKS_2D9PT>(o, wx, wy);
+    case PERKS_2D25PT: return min_domain_rows<T, PERKS_2D25PT>(o, wx, wy);
+    default: return fail(PERKS_ERR_INVALID_ARG, "not a 2D shape: " + std::to_string(shape));
+  }
+}
+
+}  // namespace perks
+
+using namespace perks;
+
+extern "C" {
+
+int perks_stencil2d_min_domain(const perks_stencil_opts* o, int wx, int* wy) {
+  if (!o || !wy) return fail(PERKS_ERR_INVALID_ARG, "NULL argument");
+  if (o->dtype != PERKS_FP32 && o->dtype != PERKS_FP64)
+    return fail(PERKS_ERR_INVALID_ARG, "stencil dtype must be PERKS_FP32 or PERKS_FP64");
+  if (o->kernel != PERKS_KERNEL_PERSISTENT && o->kernel != PERKS_KERNEL_PER_STEP)
+    return fail(PERKS_ERR_INVALID_ARG, "unknown kernel kind");
+  if (wx <= 0) return fail(PERKS_ERR_INVALID_ARG, "width_x must be positive");
+  *wy = 0;
+  return o->dtype == PERKS_FP32 ? min_domain_2d<float>(o->shape, *o, wx, wy)
+                                : min_domain_2d<double>(o->shape, *o, wx, wy);
+}
+
+int perks_get_min_width_y(int shape, int dtype, int wx, int, int, int useSM, int, int) {
+  perks_stencil_opts o;
+  perks_stencil_default_opts(&o, shape, dtype);
+  o.cache_rows = useSM ? -1 : 0;
+  int wy = 0;
+  const int rc = perks_stencil2d_min_domain(&o, wx, &wy);
+  return rc == PERKS_OK ? wy : rc;
+}
+
+}  // extern "C"

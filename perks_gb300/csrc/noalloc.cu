@@ -34,7 +34,7 @@
 #include <mutex>
 #include <string>
 #include "runtime.cuh"
-#include "stencil2d.cuh"
+#include "stencil2d_host.cuh"
 
 namespace perks {
 
@@ -85,12 +85,7 @@ static int noalloc2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
                                            " bytes of scratch, the static array holds " +
                                            std::to_string(kNoAllocScratchBytes));
   int C = 0;
-  if (persistent && o.cache_rows != 0 && steps > 1) {
-    long long avail = (long long)dev->smem_optin - (long long)Cf::ring_bytes - 256;
-    int cmax = int(std::max<long long>(0, avail / (long long)Cf::res_row_bytes));
-    if (o.cache_rows > 0) cmax = std::min(cmax, o.cache_rows);
-    C = std::max(0, std::min(cmax, tymax - 2 * H));
-  }
+  if (steps > 1) C = std::max(0, std::min(max_cache_rows<T, SHAPE>(o, *dev), tymax - 2 * H));
   const size_t smem = Cf::ring_bytes + size_t(C) * Cf::res_row_bytes;
   if (st) {
     *st = perks_stencil_stats{};

@@ -81,6 +81,25 @@ def stencil3d(field, shape: str, steps: int, out=None, **kw):
     return out, _stats(st)
 
 
+def min_domain_2d(shape: str, width_x: int, dtype=np.float32, **kw) -> int:
+    """Largest width_y that the persistent 2D kernel keeps on chip between
+    steps for this width_x (the reference's --small mode, getMinWidthY,
+    stencil/2dstencil/jacobi-2d.cu:79-136); 0 when the options cache nothing."""
+    o = _opts(shape, dtype, **kw)
+    wy = ctypes.c_int(0)
+    N.check(N.lib().perks_stencil2d_min_domain(ctypes.byref(o), int(width_x), ctypes.byref(wy)))
+    return wy.value
+
+
+def getMinWidthY(width_x: int, bdimx: int = 256, registers: int = 0, useSM: bool = True, blkpsm: int = 0,
+                 isDoubleTile: bool = False, *, shape: str = "2d5pt", dtype=np.float32) -> int:
+    """Reference signature (stencil/2dstencil/common/jacobi_cuda.cuh:14): the
+    minimum-domain width_y, or a negative status."""
+    dt = N.FP64 if np.dtype(dtype) == np.float64 else N.FP32
+    return N.lib().perks_get_min_width_y(N.SHAPES[shape], dt, int(width_x), bdimx, registers, int(useSM),
+                                         blkpsm, int(isDoubleTile))
+
+
 def jacobi_iterative(h_input: np.ndarray, width_y: int, width_x: int, output: np.ndarray, bdimx: int = 256,
                      blkpsm: int = 0, iteration: int = 3, async_: bool = False, useSM: bool = True,
                      usewarmup: bool = False, warmupiteration: int = -1, isDoubleTile: bool = False, *,
@@ -100,6 +119,11 @@ def j3d_iterative(h_input: np.ndarray, height: int, width_y: int, width_x: int, 
                   usewarmup: bool = False, warmupiteration: int = -1, isDoubleTile: bool = False,
                   getminHeight: bool = False, *, shape: str = "3d7pt") -> int:
     """Reference host API (j3d.cu:129): host arrays in and out, int status."""
+    if getminHeight:
+        is64 = h_input is not None and np.dtype(h_input.dtype) == np.float64
+        fn = N.lib().perks_j3d_iterative_f64 if is64 else N.lib().perks_j3d_iterative_f32
+        return fn(N.SHAPES[shape], None, height, width_y, width_x, None, bdimx, blkpsm, iteration,
+                  int(useSM), 0, warmupiteration, int(isDoubleTile), 1)
     if h_input.dtype not in (np.float32, np.float64) or output.dtype != h_input.dtype:
         raise TypeError("float32 or float64 arrays of one dtype")
     fn = N.lib().perks_j3d_iterative_f64 if h_input.dtype == np.float64 else N.lib().perks_j3d_iterative_f32

@@ -73,7 +73,7 @@ def test_enum_values_match_header(native):
 
 def test_status_strings_and_version(native):
     L = native.lib()
-    assert L.perks_abi_version() == 1
+    assert L.perks_abi_version() == 2
     assert L.perks_status_string(0) == b"ok"
     assert L.perks_status_string(-15) == b"device-side wait timed out"
 
