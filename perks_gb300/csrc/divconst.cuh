@@ -23,9 +23,18 @@
 // second candidate: the fma then always lands on the neighbour away from q0,
 // which is kept when its last bit is even and replaced by q0 otherwise.
 //
-// The float version is checked against IEEE division for all 2^32 inputs
-// with b = 118 and b = 159 (zero mismatches), the double version through the
-// bit-exact stencil tests on subnormal, tiny, huge, infinite and NaN fields.
+// FIN = 1 selects an equivalent form without the sign transfer: the remainder
+// is formed negated, e' = fma(q0, b, -x), and q1 = fma(e', -r, q0). Then for
+// x = -0 (q0 = -0, e' = +0) the correction adds e' * -r = -0 to -0, and a
+// quotient that underflows keeps the sign of the nonzero product e' * -r, so
+// zero results already carry the sign of x. Both forms give identical
+// results; which one ptxas schedules better differs between stencil shapes,
+// so the 2D kernels take FIN from their measured tuning table.
+//
+// The float version (both forms) is checked against IEEE division for all
+// 2^32 inputs with b = 118, 159, 59, 6 and 2 (zero mismatches, signs of zero
+// included), the double version through the bit-exact stencil tests on
+// subnormal, tiny, huge, infinite and NaN fields.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -53,35 +62,67 @@ __device__ __forceinline__ float div_finish(float x, float q0, float e, float q1
   return isfinite(q0) ? copysignf(q1, x) : q0;
 }
 
+// FIN = 1: e' = -e and q1 from it; zero results need no sign transfer.
 template <int B>
+__device__ __forceinline__ float div_finish_neg(float q0, float ep, float q1) {
+  bool keep_q0 = !isfinite(q0);  // x infinite or NaN (e' is NaN)
+  if constexpr ((B & 1) == 0) {
+    constexpr float half = float(B / 2) * 0x1p-149f;
+    const bool tie = fabsf(ep) == half;
+    constexpr bool far_on_tie = double(B) * double(1.0f / float(B)) > 1.0;
+    if constexpr (far_on_tie) {
+      keep_q0 = keep_q0 || (tie && (__float_as_uint(q1) & 1u));
+    } else {
+      const float up = __fsub_rn(q0, copysignf(0x1p-149f, ep));  // neighbour towards x/b
+      q1 = tie ? ((__float_as_uint(q0) & 1u) ? up : q0) : q1;
+    }
+  }
+  return keep_q0 ? q0 : q1;
+}
+
+template <int B, int FIN = 0>
 __device__ __forceinline__ float div_const(float x) {
   constexpr float b = float(B);
   const float r = __fdiv_rn(1.0f, b);  // folded to a constant
   const float q0 = __fmul_rn(x, r);
-  const float e = __fmaf_rn(-q0, b, x);
-  const float q1 = __fmaf_rn(e, r, q0);
-  return div_finish<B>(x, q0, e, q1);
+  if constexpr (FIN == 1) {
+    const float ep = __fmaf_rn(q0, b, -x);
+    return div_finish_neg<B>(q0, ep, __fmaf_rn(ep, -r, q0));
+  } else {
+    const float e = __fmaf_rn(-q0, b, x);
+    const float q1 = __fmaf_rn(e, r, q0);
+    return div_finish<B>(x, q0, e, q1);
+  }
 }
 
 // Two elements at once: the three rounding steps as packed FP32 pairs (each
 // half an IEEE round-to-nearest operation, so each element's result is the
 // one above), the finish per element.
-template <int B>
+template <int B, int FIN = 0>
 __device__ __forceinline__ F2 div_const(F2 x) {
   constexpr float b = float(B);
   const float r = __fdiv_rn(1.0f, b);
   const F2 q0 = RN<F2>::mul(x, F2(r));
-  const F2 e = RN<F2>::fma(q0, F2(-b), x);  // -q0*b + x, the negation exact
-  const F2 q1 = RN<F2>::fma(e, F2(r), q0);
-  float xa, xb, q0a, q0b, ea, eb, q1a, q1b;
-  x.unpack(xa, xb);
+  float q0a, q0b, ea, eb, q1a, q1b;
   q0.unpack(q0a, q0b);
-  e.unpack(ea, eb);
-  q1.unpack(q1a, q1b);
-  return F2::pack(div_finish<B>(xa, q0a, ea, q1a), div_finish<B>(xb, q0b, eb, q1b));
+  if constexpr (FIN == 1) {
+    const F2 ep = RN<F2>::fma(q0, F2(b), RN<F2>::mul(x, F2(-1.0f)));  // q0*b - x
+    const F2 q1 = RN<F2>::fma(ep, F2(-r), q0);
+    ep.unpack(ea, eb);
+    q1.unpack(q1a, q1b);
+    return F2::pack(div_finish_neg<B>(q0a, ea, q1a), div_finish_neg<B>(q0b, eb, q1b));
+  } else {
+    const F2 e = RN<F2>::fma(q0, F2(-b), x);  // -q0*b + x, the negation exact
+    const F2 q1 = RN<F2>::fma(e, F2(r), q0);
+    float xa, xb;
+    x.unpack(xa, xb);
+    e.unpack(ea, eb);
+    q1.unpack(q1a, q1b);
+    return F2::pack(div_finish<B>(xa, q0a, ea, q1a), div_finish<B>(xb, q0b, eb, q1b));
+  }
 }
 
-template <int B>
+template <int B, int FIN = 0>
 __device__ __forceinline__ double div_const(double x) {
   // FP64 arithmetic is scarce on this GPU: the tie and finiteness
   // tests and the sign transfer use integer operations on the bit patterns.
@@ -89,6 +130,19 @@ __device__ __forceinline__ double div_const(double x) {
   constexpr long long kAbs = 0x7fffffffffffffffll, kExp = 0x7ff0000000000000ll, kSign = (long long)0x8000000000000000ull;
   const double r = __ddiv_rn(1.0, b);
   const double q0 = __dmul_rn(x, r);
+  if constexpr (FIN == 1) {  // negated remainder: no sign transfer
+    const double ep = __fma_rn(q0, b, -x);
+    double q1 = __fma_rn(ep, -r, q0);
+    const long long q0b = __double_as_longlong(q0);
+    if constexpr ((B & 1) == 0) {
+      constexpr double half = double(B / 2) * 0x1p-1074;
+      if ((__double_as_longlong(ep) & kAbs) == __double_as_longlong(half)) {
+        const double up = __dsub_rn(q0, copysign(0x1p-1074, ep));
+        q1 = (q0b & 1ll) ? up : q0;
+      }
+    }
+    return ((q0b & kExp) == kExp) ? q0 : q1;
+  }
   const double e = __fma_rn(-q0, b, x);
   double q1 = __fma_rn(e, r, q0);
   const long long xb = __double_as_longlong(x), q0b = __double_as_longlong(q0);

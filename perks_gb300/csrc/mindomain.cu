@@ -9,17 +9,23 @@
 
 namespace perks {
 
+template <class T, int SHAPE>
+static int min_rows(const perks_stencil_opts& o, int wx, int* wy) {
+  return o.order == PERKS_ORDER_FAST ? min_domain_rows<Cfg2D<T, SHAPE, true>>(o, wx, wy)
+                                     : min_domain_rows<Cfg2D<T, SHAPE, false>>(o, wx, wy);
+}
+
 template <class T>
 static int min_domain_2d(int shape, const perks_stencil_opts& o, int wx, int* wy) {
   switch (shape) {
-    case PERKS_2D5PT: return min_domain_rows<T, PERKS_2D5PT>(o, wx, wy);
-    case PERKS_2DS9PT: return min_domain_rows<T, PERKS_2DS9PT>(o, wx, wy);
-    case PERKS_2D13PT: return min_domain_rows<T, PERKS_2D13PT>(o, wx, wy);
-    case PERKS_2D17PT: return min_domain_rows<T, PERKS_2D17PT>(o, wx, wy);
-    case PERKS_2D21PT: return min_domain_rows<T, PERKS_2D21PT>(o, wx, wy);
-    case PERKS_2DS25PT: return min_domain_rows<T, PERKS_2DS25PT>(o, wx, wy);
-    case PERKS_2D9PT: return min_domain_rows<T, PERKS_2D9PT>(o, wx, wy);
-    case PERKS_2D25PT: return min_domain_rows<T, PERKS_2D25PT>(o, wx, wy);
+    case PERKS_2D5PT: return min_rows<T, PERKS_2D5PT>(o, wx, wy);
+    case PERKS_2DS9PT: return min_rows<T, PERKS_2DS9PT>(o, wx, wy);
+    case PERKS_2D13PT: return min_rows<T, PERKS_2D13PT>(o, wx, wy);
+    case PERKS_2D17PT: return min_rows<T, PERKS_2D17PT>(o, wx, wy);
+    case PERKS_2D21PT: return min_rows<T, PERKS_2D21PT>(o, wx, wy);
+    case PERKS_2DS25PT: return min_rows<T, PERKS_2DS25PT>(o, wx, wy);
+    case PERKS_2D9PT: return min_rows<T, PERKS_2D9PT>(o, wx, wy);
+    case PERKS_2D25PT: return min_rows<T, PERKS_2D25PT>(o, wx, wy);
     default: return fail(PERKS_ERR_INVALID_ARG, "not a 2D shape: " + std::to_string(shape));
   }
 }
@@ -36,6 +42,8 @@ int perks_stencil2d_min_domain(const perks_stencil_opts* o, int wx, int* wy) {
     return fail(PERKS_ERR_INVALID_ARG, "stencil dtype must be PERKS_FP32 or PERKS_FP64");
   if (o->kernel != PERKS_KERNEL_PERSISTENT && o->kernel != PERKS_KERNEL_PER_STEP)
     return fail(PERKS_ERR_INVALID_ARG, "unknown kernel kind");
+  if (o->order != PERKS_ORDER_REFERENCE && o->order != PERKS_ORDER_FAST)
+    return fail(PERKS_ERR_INVALID_ARG, "unknown evaluation order");
   if (wx <= 0) return fail(PERKS_ERR_INVALID_ARG, "width_x must be positive");
   *wy = 0;
   return o->dtype == PERKS_FP32 ? min_domain_2d<float>(o->shape, *o, wx, wy)

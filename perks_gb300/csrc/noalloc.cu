@@ -64,7 +64,7 @@ static int noalloc_scratch(void** out) {
 template <class T, int SHAPE, bool FAST>
 static int noalloc2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int wy, int wx, int steps,
                      perks_stencil_stats* st) {
-  using Cf = Cfg2D<T, SHAPE>;
+  using Cf = Cfg2D<T, SHAPE, FAST>;
   constexpr int H = Cf::H;
   const DeviceInfo* dev = device_info();
   if (!dev) return PERKS_ERR_NO_DEVICE;
@@ -85,7 +85,7 @@ static int noalloc2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
                                            " bytes of scratch, the static array holds " +
                                            std::to_string(kNoAllocScratchBytes));
   int C = 0;
-  if (steps > 1) C = std::max(0, std::min(max_cache_rows<T, SHAPE>(o, *dev), tymax - 2 * H));
+  if (steps > 1) C = std::max(0, std::min(max_cache_rows<Cf>(o, *dev), tymax - 2 * H));
   const size_t smem = Cf::ring_bytes + size_t(C) * Cf::res_row_bytes;
   if (st) {
     *st = perks_stencil_stats{};
@@ -126,7 +126,7 @@ static int noalloc2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   p.persistent = persistent;
   p.bar = words;
   p.status = words + 2;
-  auto kern = stencil2d_kernel<T, SHAPE, FAST>;
+  auto kern = stencil2d_kernel<T, SHAPE, FAST, Cf>;
   PERKS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   if (persistent) {
     int per_sm = 0;

@@ -95,7 +95,7 @@ __host__ __device__ constexpr double c27(int z, int y, int x) {
 // east, north, each term a rounded product added to the rounded running sum,
 // then / 118. `add(acc, p)` is the rounded sum (a packed-pair caller passes a
 // form ptxas cannot fuse with the product).
-template <class T, int SHAPE, class U, class Add>
+template <class T, int SHAPE, int FIN = 0, class U, class Add>
 __device__ __forceinline__ T star2d_ref(const U& u, const Add& add) {
   using O = RN<T>;
   constexpr int H = ShapeInfo<SHAPE>::H;
@@ -109,15 +109,15 @@ __device__ __forceinline__ T star2d_ref(const U& u, const Add& add) {
   for (int h = 0; h < H; h++) acc = add(acc, O::mul(T(star_e(h)), u(0, 0, 1 + h)));
 #pragma unroll
   for (int h = 0; h < H; h++) acc = add(acc, O::mul(T(star_n(h)), u(0, 1 + h, 0)));
-  return div_const<118>(acc);
+  return div_const<118, FIN>(acc);
 }
 
-template <class T, int SHAPE, class U>
+template <class T, int SHAPE, int FIN = 0, class U>
 __device__ __forceinline__ T point_ref(const U& u) {
   using O = RN<T>;
   constexpr int H = ShapeInfo<SHAPE>::H;
   if constexpr (SHAPE <= PERKS_2DS25PT) {
-    return star2d_ref<T, SHAPE>(u, [](T a, T b) { return O::add(a, b); });
+    return star2d_ref<T, SHAPE, FIN>(u, [](T a, T b) { return O::add(a, b); });
   } else if constexpr (SHAPE == PERKS_2D9PT || SHAPE == PERKS_2D25PT) {
     // Terms before the centre sum in T; the centre's double literal promotes
     // the rest of the sum to double; later products are still T products.
@@ -140,7 +140,7 @@ __device__ __forceinline__ T point_ref(const U& u) {
         }
       }
     }
-    return T(div_const<118>(accd));
+    return T(div_const<118, FIN>(accd));
   } else if constexpr (SHAPE == PERKS_3D7PT) {
     // e, w, n, s, t, b then minus the centre; float-literal coefficients.
     T acc = O::mul(T(0.161f), u(0, 0, 1));
@@ -184,7 +184,7 @@ __device__ __forceinline__ T point_ref(const U& u) {
     ct = O::add(ct, u(1, 1, -1));
     ct = O::add(ct, u(1, 1, 1));
     acc = D::add(acc, D::mul(0.52, double(ct)));
-    return T(div_const<159>(acc));
+    return T(div_const<159, FIN>(acc));
   } else if constexpr (SHAPE == PERKS_3D27PT) {
     using D = RN<double>;
     double acc = 0.0;
@@ -197,7 +197,7 @@ __device__ __forceinline__ T point_ref(const U& u) {
           const double t = D::mul(c27(z, y, x), double(u(z - 1, y - 1, x - 1)));
           acc = (z == 0 && y == 0 && x == 0) ? t : D::add(acc, t);
         }
-    return T(div_const<159>(acc));
+    return T(div_const<159, FIN>(acc));
   } else {  // PERKS_POISSON
     T f = O::add(u(-1, 0, 0), u(1, 0, 0));
     f = O::add(f, u(0, -1, 0));
@@ -289,12 +289,12 @@ __device__ __forceinline__ T point_fast(const U& u) {
   }
 }
 
-template <class T, int SHAPE, bool FAST, class U>
+template <class T, int SHAPE, bool FAST, int FIN = 0, class U>
 __device__ __forceinline__ T stencil_point(const U& u) {
   if constexpr (FAST)
     return point_fast<T, SHAPE>(u);
   else
-    return point_ref<T, SHAPE>(u);
+    return point_ref<T, SHAPE, FIN>(u);
 }
 
 }  // namespace perks

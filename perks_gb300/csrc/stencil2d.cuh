@@ -32,6 +32,7 @@
 #include <type_traits>
 #include "ptx.cuh"
 #include "shapes.cuh"
+#include "tune2d.cuh"
 
 namespace perks {
 
@@ -47,8 +48,9 @@ struct Stencil2DParams {
   float one = 1.0f;  // 1.0 the compiler cannot see (packed FP32 sums, see f32x2.cuh)
 };
 
+// Shape geometry and the built-in choice of warps per CTA.
 template <class T, int SHAPE>
-struct Cfg2D {
+struct Geom2D {
   static constexpr int H = ShapeInfo<SHAPE>::H;
   static constexpr bool BOX = ShapeInfo<SHAPE>::box;
   static constexpr int V16 = 16 / sizeof(T);             // elements per 16-byte vector
@@ -65,17 +67,53 @@ struct Cfg2D {
   // FP32 star shapes of radius 2 and 3: 12 warps (168 registers per thread)
   // measured faster than 16 (128 registers) and 8 on GB300 (2ds9pt 686 vs 662
   // GCells/s, 2d13pt 487 vs 416, reference order, 8192^2)
-  static constexpr int NW = (sizeof(T) == 4 && !BOX && (H == 2 || H == 3)) ? 12 : NW_REG;
-  static constexpr int NT = NW * 32;
-  static constexpr int D = NW >= 24 ? 3 : NW == 16 ? 4 : 6;  // rows in flight per warp
-  static constexpr int DR = D + 1;                       // ring slots per warp
-  static constexpr int SLOT = SW + 2 * H * V16;          // ring slot: strip row + one chunk per edge lane
-  static constexpr size_t ring_bytes = size_t(NW) * DR * SLOT * sizeof(T);
-  static constexpr size_t res_row_bytes = size_t(NW) * SW * sizeof(T);  // one resident row for every warp
-  static_assert(2 * H <= 32, "edge lanes");
+  static constexpr int NW_DEF = (sizeof(T) == 4 && !BOX && (H == 2 || H == 3)) ? 12 : NW_REG;
+  static constexpr int d_def(int nw) { return nw >= 24 ? 3 : nw == 16 ? 4 : 6; }
   // FP32 star shapes in the reference order run their arithmetic on packed pairs
   static constexpr bool PAIR = sizeof(T) == 4 && !BOX && SHAPE <= PERKS_2DS25PT;
 };
+
+// Warps per CTA, rows in flight and division form for one kernel: the
+// measured table (tune2d.cuh), else the built-in choice. The tuning tool
+// overrides all three for a whole translation unit with PERKS_TUNE_*.
+template <class T, int SHAPE, bool FAST>
+struct Pick2D {
+  static constexpr Tune2D t = kTune2D[sizeof(T) == 8][FAST][SHAPE];
+#ifdef PERKS_TUNE_NW
+  static constexpr int NW = PERKS_TUNE_NW;
+#else
+  static constexpr int NW = t.nw ? t.nw : Geom2D<T, SHAPE>::NW_DEF;
+#endif
+#ifdef PERKS_TUNE_D
+  static constexpr int D = PERKS_TUNE_D;
+#else
+  static constexpr int D = t.d ? t.d : Geom2D<T, SHAPE>::d_def(NW);
+#endif
+#ifdef PERKS_TUNE_FIN
+  static constexpr int FIN = FAST ? 0 : PERKS_TUNE_FIN;
+#else
+  static constexpr int FIN = FAST ? 0 : t.fin;
+#endif
+};
+
+// Full configuration. The chosen values are template arguments, so kernels
+// built with different choices never share a name.
+template <class T, int SHAPE, int NW_, int D_, int FIN_>
+struct Cfg2DT : Geom2D<T, SHAPE> {
+  using G = Geom2D<T, SHAPE>;
+  static constexpr int NW = NW_;
+  static constexpr int NT = NW * 32;
+  static constexpr int D = D_;                           // rows in flight per warp
+  static constexpr int DR = D + 1;                       // ring slots per warp
+  static constexpr int FIN = FIN_;                       // division form (divconst.cuh)
+  static constexpr int SLOT = G::SW + 2 * G::H * G::V16; // ring slot: strip row + one chunk per edge lane
+  static constexpr size_t ring_bytes = size_t(NW) * DR * SLOT * sizeof(T);
+  static constexpr size_t res_row_bytes = size_t(NW) * G::SW * sizeof(T);  // one resident row for every warp
+  static_assert(2 * G::H <= 32, "edge lanes");
+  static_assert(NW >= 1 && NW <= 32 && D >= 1 && D <= 8, "launch shape");
+};
+template <class T, int SHAPE, bool FAST = false>
+using Cfg2D = Cfg2DT<T, SHAPE, Pick2D<T, SHAPE, FAST>::NW, Pick2D<T, SHAPE, FAST>::D, Pick2D<T, SHAPE, FAST>::FIN>;
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, uint64_t pol) {
   asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(smem_u32(smem)), "l"(gmem),
@@ -138,9 +176,8 @@ __device__ __forceinline__ void static_for(F&& f) {
   }
 }
 
-template <class T, int SHAPE, bool FAST>
-__global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const __grid_constant__ Stencil2DParams p) {
-  using Cf = Cfg2D<T, SHAPE>;
+template <class T, int SHAPE, bool FAST, class Cf>
+__global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_constant__ Stencil2DParams p) {
   constexpr int H = Cf::H, V = Cf::V, V16 = Cf::V16, NV = Cf::NV, SW = Cf::SW, NW = Cf::NW, D = Cf::D,
                 DR = Cf::DR, SLOT = Cf::SLOT;
   constexpr int WN = Cf::WN;
@@ -330,7 +367,7 @@ __global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const
                     if (dy == 0) return F2::pack(hc.h[H + i + dx], hc.h[H + i + 1 + dx]);
                     return F2::pack(w[ws(dy)].v[i], w[ws(dy)].v[i + 1]);
                   };
-                  star2d_ref<F2, SHAPE>(u2, [one2](F2 a, F2 b) { return RN<F2>::fma(b, one2, a); })
+                  star2d_ref<F2, SHAPE, Cf::FIN>(u2, [one2](F2 a, F2 b) { return RN<F2>::fma(b, one2, a); })
                       .unpack(o[i], o[i + 1]);
                 }
               } else {
@@ -340,7 +377,7 @@ __global__ void __launch_bounds__(Cfg2D<T, SHAPE>::NT, 1) stencil2d_kernel(const
                     if constexpr (BOX) return wf[ws(dy)].h[H + i + dx];
                     else return dy == 0 ? hc.h[H + i + dx] : w[ws(dy)].v[i];
                   };
-                  o[i] = stencil_point<T, SHAPE, FAST>(u);
+                  o[i] = stencil_point<T, SHAPE, FAST, Cf::FIN>(u);
                 }
               }
               if (dir) {

@@ -13,9 +13,8 @@ inline int ceil_div(long long a, long long b) { return int((a + b - 1) / b); }
 
 // Rows per warp that the persistent kernel can keep in shared memory next to
 // its prefetch ring (0 when caching is off or the kernel is not persistent).
-template <class T, int SHAPE>
+template <class Cf>
 int max_cache_rows(const perks_stencil_opts& o, const DeviceInfo& dev) {
-  using Cf = Cfg2D<T, SHAPE>;
   if (o.kernel != PERKS_KERNEL_PERSISTENT || o.cache_rows == 0) return 0;
   const long long avail = (long long)dev.smem_optin - (long long)Cf::ring_bytes - 256;
   int cmax = int(std::max<long long>(0, avail / (long long)Cf::res_row_bytes));
@@ -27,9 +26,8 @@ int max_cache_rows(const perks_stencil_opts& o, const DeviceInfo& dev) {
 // H rows at each end, which go through the field as halo of the neighbouring
 // bands (the reference's getMinWidthY, stencil/2dstencil/jacobi-2d.cu:79-136:
 // cached rows per CTA x CTAs along y). 0 when nothing is cached.
-template <class T, int SHAPE>
+template <class Cf>
 int min_domain_rows(const perks_stencil_opts& o, int wx, int* wy) {
-  using Cf = Cfg2D<T, SHAPE>;
   const DeviceInfo* dev = device_info();
   if (!dev) return PERKS_ERR_NO_DEVICE;
   const int ctas = o.ctas > 0 ? std::min(o.ctas, dev->sms) : dev->sms;
@@ -38,7 +36,7 @@ int min_domain_rows(const perks_stencil_opts& o, int wx, int* wy) {
   if (ns > warps)
     return fail(PERKS_ERR_UNSUPPORTED, "width_x " + std::to_string(wx) + " needs more than " +
                                            std::to_string(warps) + " column strips");
-  const int cmax = max_cache_rows<T, SHAPE>(o, *dev);
+  const int cmax = max_cache_rows<Cf>(o, *dev);
   const long long rows = cmax > 0 ? (warps / ns) * (long long)(cmax + 2 * Cf::H) : 0;
   *wy = int(std::min<long long>(rows, 0x7fffffff));
   return PERKS_OK;
@@ -47,7 +45,7 @@ int min_domain_rows(const perks_stencil_opts& o, int wx, int* wy) {
 template <class T, int SHAPE, bool FAST>
 int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int wy, int wx, int steps,
                      perks_stencil_stats* st) {
-  using Cf = Cfg2D<T, SHAPE>;
+  using Cf = Cfg2D<T, SHAPE, FAST>;
   constexpr int H = Cf::H;
   const DeviceInfo* dev = device_info();
   if (!dev) return PERKS_ERR_NO_DEVICE;
@@ -65,7 +63,7 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   const int grid = ceil_div((long long)ns * nb, Cf::NW);
 
   int C = 0;
-  if (steps > 1) C = std::max(0, std::min(max_cache_rows<T, SHAPE>(o, *dev), tymax - 2 * H));
+  if (steps > 1) C = std::max(0, std::min(max_cache_rows<Cf>(o, *dev), tymax - 2 * H));
   const size_t smem = Cf::ring_bytes + size_t(C) * Cf::res_row_bytes;
   if (smem > dev->smem_optin) return fail(PERKS_ERR_UNSUPPORTED, "shared memory budget exceeded");
 
@@ -112,7 +110,7 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   p.bar = sw.bar;
   p.status = sw.status;
 
-  auto kern = stencil2d_kernel<T, SHAPE, FAST>;
+  auto kern = stencil2d_kernel<T, SHAPE, FAST, Cf>;
   PERKS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   cudaEvent_t e0, e1;
   PERKS_CUDA(cudaEventCreate(&e0));
