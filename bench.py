@@ -297,6 +297,7 @@ def main():
         extra["persistent_fast_fp64_gcells"] = round(st["gcells_per_s"], 2)
         del d64, o64
         extra["cached_fraction"] = round(kernel_cached_fraction(P, d_in, d_out), 4)
+        extra.update(host_link_gbs(torch, host, hout, d_in, d_out))
         extra.update(extra_min_domain(P, torch))
         extra.update(extra_3d(P, torch))
         extra.update(extra_cg(P, torch))
@@ -326,6 +327,21 @@ def main():
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def host_link_gbs(torch, host, hout, d_in, d_out, reps=5):
+    """Pinned host <-> device copy rate of one field (the ceiling of the e2e copies)."""
+    out = {}
+    for tag, dst, src in (("h2d_gbs", d_in, host), ("d2h_gbs", hout, d_out)):
+        dst.copy_(src, non_blocking=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            dst.copy_(src, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        out[tag] = round(src.numel() * src.element_size() * reps / (e0.elapsed_time(e1) * 1e6), 1)
+    return out
 
 
 def extra_min_domain(P, torch, steps=1000):

@@ -8,14 +8,14 @@
 namespace perks {
 #define PERKS_DECL_2D(sfx)                                                                            \
   int stencil2d_##sfx(int shape, const perks_stencil_opts& o, const void* in, void* out, int wy, int wx, \
-                      int steps, perks_stencil_stats* st);
+                      int steps, perks_stencil_stats* st, bool host_io);
 PERKS_DECL_2D(f32_ref)
 PERKS_DECL_2D(f32_fast)
 PERKS_DECL_2D(f64_ref)
 PERKS_DECL_2D(f64_fast)
 #define PERKS_DECL_3D(sfx)                                                                              \
   int stencil3d_##sfx(int shape, const perks_stencil_opts& o, const void* in, void* out, int h, int wy, \
-                      int wx, int steps, perks_stencil_stats* st);
+                      int wx, int steps, perks_stencil_stats* st, bool host_io);
 PERKS_DECL_3D(f32_ref)
 PERKS_DECL_3D(f32_fast)
 PERKS_DECL_3D(f64_ref)
@@ -40,35 +40,43 @@ static int check_opts(const perks_stencil_opts* o, bool want3d) {
   return PERKS_OK;
 }
 
-// Host-buffer round trip used by the reference-signature drop-ins.
+static int run2d(const perks_stencil_opts& o, const void* in, void* out, int wy, int wx, int steps,
+                 perks_stencil_stats* st, bool host_io) {
+  const bool fast = o.order == PERKS_ORDER_FAST;
+  if (o.dtype == PERKS_FP32)
+    return fast ? stencil2d_f32_fast(o.shape, o, in, out, wy, wx, steps, st, host_io)
+                : stencil2d_f32_ref(o.shape, o, in, out, wy, wx, steps, st, host_io);
+  return fast ? stencil2d_f64_fast(o.shape, o, in, out, wy, wx, steps, st, host_io)
+              : stencil2d_f64_ref(o.shape, o, in, out, wy, wx, steps, st, host_io);
+}
+
+static int run3d(const perks_stencil_opts& o, const void* in, void* out, int h, int wy, int wx, int steps,
+                 perks_stencil_stats* st, bool host_io) {
+  const bool fast = o.order == PERKS_ORDER_FAST;
+  if (o.dtype == PERKS_FP32)
+    return fast ? stencil3d_f32_fast(o.shape, o, in, out, h, wy, wx, steps, st, host_io)
+                : stencil3d_f32_ref(o.shape, o, in, out, h, wy, wx, steps, st, host_io);
+  return fast ? stencil3d_f64_fast(o.shape, o, in, out, h, wy, wx, steps, st, host_io)
+              : stencil3d_f64_ref(o.shape, o, in, out, h, wy, wx, steps, st, host_io);
+}
+
+// Host-buffer round trip used by the reference-signature drop-ins: the field
+// is copied from h_in straight into the library's internal field and the
+// result straight back into h_out (no staging buffers, nothing allocated per
+// call once the workspace has grown to the field size).
 template <class T>
 static int host_roundtrip(const perks_stencil_opts& o, const T* h_in, T* h_out, int h, int wy, int wx,
                           int iteration, int usewarmup, int warmupiteration) {
-  const size_t n = size_t(h) * wy * wx;
-  T *d_in = nullptr, *d_out = nullptr;
-  PERKS_CUDA(cudaMalloc(&d_in, n * sizeof(T)));
-  cudaError_t e = cudaMalloc(&d_out, n * sizeof(T));
-  if (e != cudaSuccess) {
-    cudaFree(d_in);
-    return cuda_fail(e, "cudaMalloc");
-  }
+  if ((long long)h * wy * wx > (1ll << 40)) return fail(PERKS_ERR_INVALID_ARG, "domain too large");
   int rc = PERKS_OK;
-  e = cudaMemcpy(d_in, h_in, n * sizeof(T), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpy H2D");
-  if (rc == PERKS_OK && usewarmup) {
-    int wi = warmupiteration > 0 ? warmupiteration : iteration;
-    rc = (h == 1 && !is3d(o.shape)) ? perks_stencil2d(&o, d_in, d_out, wy, wx, wi, nullptr)
-                                    : perks_stencil3d(&o, d_in, d_out, h, wy, wx, wi, nullptr);
+  const bool two = h == 1 && !is3d(o.shape);
+  if (usewarmup) {
+    const int wi = warmupiteration > 0 ? warmupiteration : iteration;
+    rc = two ? run2d(o, h_in, h_out, wy, wx, wi, nullptr, true) : run3d(o, h_in, h_out, h, wy, wx, wi, nullptr, true);
   }
   if (rc == PERKS_OK)
-    rc = (h == 1 && !is3d(o.shape)) ? perks_stencil2d(&o, d_in, d_out, wy, wx, iteration, nullptr)
-                                    : perks_stencil3d(&o, d_in, d_out, h, wy, wx, iteration, nullptr);
-  if (rc == PERKS_OK) {
-    e = cudaMemcpy(h_out, d_out, n * sizeof(T), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpy D2H");
-  }
-  cudaFree(d_in);
-  cudaFree(d_out);
+    rc = two ? run2d(o, h_in, h_out, wy, wx, iteration, nullptr, true)
+             : run3d(o, h_in, h_out, h, wy, wx, iteration, nullptr, true);
   return rc;
 }
 
@@ -101,12 +109,7 @@ int perks_stencil2d(const perks_stencil_opts* o, const void* d_in, void* d_out, 
   if (!d_in || !d_out) return fail(PERKS_ERR_INVALID_ARG, "null device pointer");
   if (wy <= 0 || wx <= 0 || steps < 0) return fail(PERKS_ERR_INVALID_ARG, "sizes must be positive, steps >= 0");
   if ((long long)wy * wx > (1ll << 40)) return fail(PERKS_ERR_INVALID_ARG, "domain too large");
-  const bool fast = o->order == PERKS_ORDER_FAST;
-  if (o->dtype == PERKS_FP32)
-    return fast ? stencil2d_f32_fast(o->shape, *o, d_in, d_out, wy, wx, steps, st)
-                : stencil2d_f32_ref(o->shape, *o, d_in, d_out, wy, wx, steps, st);
-  return fast ? stencil2d_f64_fast(o->shape, *o, d_in, d_out, wy, wx, steps, st)
-              : stencil2d_f64_ref(o->shape, *o, d_in, d_out, wy, wx, steps, st);
+  return run2d(*o, d_in, d_out, wy, wx, steps, st, false);
 }
 
 int perks_stencil3d(const perks_stencil_opts* o, const void* d_in, void* d_out, int h, int wy, int wx, int steps,
@@ -116,12 +119,7 @@ int perks_stencil3d(const perks_stencil_opts* o, const void* d_in, void* d_out, 
   if (!d_in || !d_out) return fail(PERKS_ERR_INVALID_ARG, "null device pointer");
   if (h <= 0 || wy <= 0 || wx <= 0 || steps < 0)
     return fail(PERKS_ERR_INVALID_ARG, "sizes must be positive, steps >= 0");
-  const bool fast = o->order == PERKS_ORDER_FAST;
-  if (o->dtype == PERKS_FP32)
-    return fast ? stencil3d_f32_fast(o->shape, *o, d_in, d_out, h, wy, wx, steps, st)
-                : stencil3d_f32_ref(o->shape, *o, d_in, d_out, h, wy, wx, steps, st);
-  return fast ? stencil3d_f64_fast(o->shape, *o, d_in, d_out, h, wy, wx, steps, st)
-              : stencil3d_f64_ref(o->shape, *o, d_in, d_out, h, wy, wx, steps, st);
+  return run3d(*o, d_in, d_out, h, wy, wx, steps, st, false);
 }
 
 static int jacobi_common(int shape, int dtype, const void* h_in, int wy, int wx, void* h_out, int iteration,

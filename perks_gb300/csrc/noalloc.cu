@@ -110,8 +110,8 @@ static int noalloc2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   unsigned* words = reinterpret_cast<unsigned*>(b + 2 * fbytes);
   // barrier and status words must start at zero; the array keeps old contents
   PERKS_CUDA(cudaMemsetAsync(words, 0, 4 * sizeof(unsigned), s));
-  PERKS_CUDA(cudaMemcpy2DAsync(f0, size_t(pitch) * sizeof(T), d_in, size_t(wx) * sizeof(T), size_t(wx) * sizeof(T),
-                               wy, cudaMemcpyDeviceToDevice, s));
+  PERKS_CUDA(copy_rows(f0, size_t(pitch) * sizeof(T), d_in, size_t(wx) * sizeof(T), size_t(wx) * sizeof(T),
+                       wy, cudaMemcpyDeviceToDevice, s));
   Stencil2DParams p{};
   p.f[0] = f0;
   p.f[1] = f1;
@@ -146,8 +146,8 @@ static int noalloc2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
     PERKS_CUDA(cudaGetLastError());
     count_launch(steps);
   }
-  PERKS_CUDA(cudaMemcpy2DAsync(d_out, size_t(wx) * sizeof(T), (steps & 1) ? f1 : f0, size_t(pitch) * sizeof(T),
-                               size_t(wx) * sizeof(T), wy, cudaMemcpyDeviceToDevice, s));
+  PERKS_CUDA(copy_rows(d_out, size_t(wx) * sizeof(T), (steps & 1) ? f1 : f0, size_t(pitch) * sizeof(T),
+                       size_t(wx) * sizeof(T), wy, cudaMemcpyDeviceToDevice, s));
   SyncWords sw{words, words + 2};
   rc = check_status(sw, s);
   if (rc != PERKS_OK) return rc;

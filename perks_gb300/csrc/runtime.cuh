@@ -36,6 +36,15 @@ void* workspace(WorkSlot slot, size_t bytes, int* status);
 
 void count_launch(int n = 1);
 
+// rows x width bytes between pitched buffers; one linear copy when both
+// pitches equal the width (a pitched copy of a dense field moves rows one
+// by one, which is slower between host and device).
+inline cudaError_t copy_rows(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t rows,
+                             cudaMemcpyKind kind, cudaStream_t s) {
+  if (dpitch == width && spitch == width) return cudaMemcpyAsync(dst, src, width * rows, kind, s);
+  return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, rows, kind, s);
+}
+
 // Device status word + grid barrier words: 4 unsigned in kWsSync.
 struct SyncWords {
   unsigned* bar;     // [2]

@@ -3,18 +3,18 @@
 
 namespace perks {
 int stencil2d_f64_ref(int shape, const perks_stencil_opts& o, const void* in, void* out, int wy, int wx,
-                          int steps, perks_stencil_stats* st) {
+                          int steps, perks_stencil_stats* st, bool host_io) {
   const double* i = static_cast<const double*>(in);
   double* q = static_cast<double*>(out);
   switch (shape) {
-    case PERKS_2D5PT: return launch_stencil2d<double, PERKS_2D5PT, false>(o, i, q, wy, wx, steps, st);
-    case PERKS_2DS9PT: return launch_stencil2d<double, PERKS_2DS9PT, false>(o, i, q, wy, wx, steps, st);
-    case PERKS_2D13PT: return launch_stencil2d<double, PERKS_2D13PT, false>(o, i, q, wy, wx, steps, st);
-    case PERKS_2D17PT: return launch_stencil2d<double, PERKS_2D17PT, false>(o, i, q, wy, wx, steps, st);
-    case PERKS_2D21PT: return launch_stencil2d<double, PERKS_2D21PT, false>(o, i, q, wy, wx, steps, st);
-    case PERKS_2DS25PT: return launch_stencil2d<double, PERKS_2DS25PT, false>(o, i, q, wy, wx, steps, st);
-    case PERKS_2D9PT: return launch_stencil2d<double, PERKS_2D9PT, false>(o, i, q, wy, wx, steps, st);
-    case PERKS_2D25PT: return launch_stencil2d<double, PERKS_2D25PT, false>(o, i, q, wy, wx, steps, st);
+    case PERKS_2D5PT: return launch_stencil2d<double, PERKS_2D5PT, false>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2DS9PT: return launch_stencil2d<double, PERKS_2DS9PT, false>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2D13PT: return launch_stencil2d<double, PERKS_2D13PT, false>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2D17PT: return launch_stencil2d<double, PERKS_2D17PT, false>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2D21PT: return launch_stencil2d<double, PERKS_2D21PT, false>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2DS25PT: return launch_stencil2d<double, PERKS_2DS25PT, false>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2D9PT: return launch_stencil2d<double, PERKS_2D9PT, false>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2D25PT: return launch_stencil2d<double, PERKS_2D25PT, false>(o, i, q, wy, wx, steps, st, host_io);
     default: return fail(PERKS_ERR_INVALID_ARG, "not a 2D shape: " + std::to_string(shape));
   }
 }

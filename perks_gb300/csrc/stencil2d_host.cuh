@@ -42,9 +42,11 @@ int min_domain_rows(const perks_stencil_opts& o, int wx, int* wy) {
   return PERKS_OK;
 }
 
+// d_in / d_out are device buffers, or host buffers when host_io is set: the
+// field then goes straight between them and the internal pitched fields.
 template <class T, int SHAPE, bool FAST>
 int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int wy, int wx, int steps,
-                     perks_stencil_stats* st) {
+                     perks_stencil_stats* st, bool host_io = false) {
   using Cf = Cfg2D<T, SHAPE, FAST>;
   constexpr int H = Cf::H;
   const DeviceInfo* dev = device_info();
@@ -78,7 +80,8 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   }
   const size_t elems = size_t(wy) * wx;
   if (steps == 0) {
-    PERKS_CUDA(cudaMemcpyAsync(d_out, d_in, elems * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    PERKS_CUDA(cudaMemcpyAsync(d_out, d_in, elems * sizeof(T), host_io ? cudaMemcpyHostToHost : cudaMemcpyDeviceToDevice,
+                               s));
     PERKS_CUDA(cudaStreamSynchronize(s));
     return PERKS_OK;
   }
@@ -92,8 +95,8 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   SyncWords sw;
   if ((stt = sync_words(&sw, s)) != PERKS_OK) return stt;
 
-  PERKS_CUDA(cudaMemcpy2DAsync(f0, size_t(pitch) * sizeof(T), d_in, size_t(wx) * sizeof(T), size_t(wx) * sizeof(T),
-                               wy, cudaMemcpyDeviceToDevice, s));
+  PERKS_CUDA(copy_rows(f0, size_t(pitch) * sizeof(T), d_in, size_t(wx) * sizeof(T), size_t(wx) * sizeof(T),
+                       wy, host_io ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
 
   Stencil2DParams p{};
   p.f[0] = f0;
@@ -152,8 +155,9 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   }
   PERKS_CUDA(cudaEventRecord(e1, s));
   count_launch(launches);
-  PERKS_CUDA(cudaMemcpy2DAsync(d_out, size_t(wx) * sizeof(T), (steps & 1) ? f1 : f0, size_t(pitch) * sizeof(T),
-                               size_t(wx) * sizeof(T), wy, cudaMemcpyDeviceToDevice, s));
+  PERKS_CUDA(copy_rows(d_out, size_t(wx) * sizeof(T), (steps & 1) ? f1 : f0, size_t(pitch) * sizeof(T),
+                       size_t(wx) * sizeof(T), wy, host_io ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                       s));
   int rc = check_status(sw, s);
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);

@@ -10,9 +10,10 @@ namespace perks {
 
 int encode_tiled_3d(CUtensorMap* map, bool f64, void* base, int wx, int wy, int h, int px, int box_x, int box_y);
 
+// d_in / d_out are device buffers, or host buffers when host_io is set.
 template <class T, int SHAPE, bool FAST>
 int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h, int wy, int wx, int steps,
-                     perks_stencil_stats* st) {
+                     perks_stencil_stats* st, bool host_io = false) {
   using Cf = Cfg3D<T, SHAPE>;
   const DeviceInfo* dev = device_info();
   if (!dev) return PERKS_ERR_NO_DEVICE;
@@ -38,7 +39,8 @@ int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h
   }
   const size_t elems = size_t(h) * wy * wx;
   if (steps == 0) {
-    PERKS_CUDA(cudaMemcpyAsync(d_out, d_in, elems * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    PERKS_CUDA(cudaMemcpyAsync(d_out, d_in, elems * sizeof(T), host_io ? cudaMemcpyHostToHost : cudaMemcpyDeviceToDevice,
+                               s));
     PERKS_CUDA(cudaStreamSynchronize(s));
     return PERKS_OK;
   }
@@ -50,8 +52,8 @@ int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h
   if (!f1) return stt;
   SyncWords sw;
   if ((stt = sync_words(&sw, s)) != PERKS_OK) return stt;
-  PERKS_CUDA(cudaMemcpy2DAsync(f0, size_t(px) * sizeof(T), d_in, size_t(wx) * sizeof(T), size_t(wx) * sizeof(T),
-                               size_t(h) * wy, cudaMemcpyDeviceToDevice, s));
+  PERKS_CUDA(copy_rows(f0, size_t(px) * sizeof(T), d_in, size_t(wx) * sizeof(T), size_t(wx) * sizeof(T),
+                       size_t(h) * wy, host_io ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
 
   Stencil3DParams p{};
   for (int i = 0; i < 2; i++) {
@@ -116,8 +118,9 @@ int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h
   }
   PERKS_CUDA(cudaEventRecord(e1, s));
   count_launch(launches);
-  PERKS_CUDA(cudaMemcpy2DAsync(d_out, size_t(wx) * sizeof(T), (steps & 1) ? f1 : f0, size_t(px) * sizeof(T),
-                               size_t(wx) * sizeof(T), size_t(h) * wy, cudaMemcpyDeviceToDevice, s));
+  PERKS_CUDA(copy_rows(d_out, size_t(wx) * sizeof(T), (steps & 1) ? f1 : f0, size_t(px) * sizeof(T),
+                       size_t(wx) * sizeof(T), size_t(h) * wy,
+                       host_io ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
   int rc = check_status(sw, s);
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);

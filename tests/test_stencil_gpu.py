@@ -196,3 +196,34 @@ def test_decay_through_subnormals(native, cuda, oracle, dt):
     steps = 140 if dt == np.float32 else 900
     g, _ = run(native, cuda, f, "2d5pt", steps)
     assert bits_equal(g, oracle.stencil("2d5pt", f, steps))
+
+
+@pytest.mark.parametrize("shape,dt,dims", [("2d5pt", np.float32, (300, 517)), ("2ds9pt", np.float32, (64, 8192)),
+                                           ("2d25pt", np.float64, (77, 1000)), ("3d7pt", np.float32, (20, 33, 70)),
+                                           ("3d27pt", np.float64, (9, 40, 130)), ("poisson", np.float32, (5, 6, 7))])
+def test_host_buffer_dropins(native, cuda, oracle, shape, dt, dims):
+    """jacobi_iterative / j3d_iterative: host arrays (pageable and pinned) in
+    and out, copied straight to and from the internal fields."""
+    import torch
+    f = np.random.default_rng(21).random(dims).astype(dt)
+    ref = oracle.stencil(shape, f, 6)
+    pinned_in = torch.from_numpy(f.copy()).pin_memory().numpy()
+    pinned_out = torch.empty(dims, dtype=torch.from_numpy(f).dtype).pin_memory().numpy()
+    for src, dst in ((f, np.empty_like(f)), (pinned_in, pinned_out)):
+        for warm in (False, True):
+            dst[...] = np.nan
+            if len(dims) == 2:
+                rc = native.jacobi_iterative(src, dims[0], dims[1], dst, iteration=6, usewarmup=warm,
+                                             warmupiteration=2, shape=shape)
+            else:
+                rc = native.j3d_iterative(src, dims[0], dims[1], dims[2], dst, iteration=6, usewarmup=warm,
+                                          warmupiteration=2, shape=shape)
+            assert rc == 0, native.last_error()
+            assert bits_equal(dst, ref), (shape, warm)
+    # zero steps copies
+    dst = np.empty_like(f)
+    if len(dims) == 2:
+        assert native.jacobi_iterative(f, dims[0], dims[1], dst, iteration=0, shape=shape) == 0
+    else:
+        assert native.j3d_iterative(f, dims[0], dims[1], dims[2], dst, iteration=0, shape=shape) == 0
+    assert bits_equal(dst, f)
