@@ -382,9 +382,10 @@ def extra_3d(P, torch):
 
 
 def extra_cg(P, torch):
-    """CG time to a 1e-10 relative residual on the 2D 5-point Laplacian,
-    2048^2 (4.19M rows, 20.96M nonzeros), RHS uniform [-1,1) seed 1, x0 = 0:
-    FP64 vs mixed precision (FP32 inner, FP64 reliable updates), CSR and DIA."""
+    """CG time to a 1e-10 relative residual, RHS uniform [-1,1) seed 1, x0 = 0,
+    FP64 vs mixed precision (FP32 inner, FP64 reliable updates): the 2D
+    5-point Laplacian 2048^2 (4.19M rows, 20.96M nonzeros) in CSR and DIA, the
+    3D 7-point Laplacian 160^3 and a random SPD matrix in CSR."""
     import numpy as np
     from perks_gb300 import matrices as M
     rp, ci, v = M.laplacian_2d(2048)
@@ -397,10 +398,21 @@ def extra_cg(P, torch):
                 x, res = P.cg_csr(rp, ci, v, b, dtype=dt, tol=1e-10)
             else:
                 x, res = P.cg_dia(off, data, b, dtype=dt, tol=1e-10)
-            out[f"cg_lap2d_2048_{fmt}_{dt}"] = {"ms": round(res["ms"], 2), "iterations": res["iterations"],
-                                                "us_per_iter": round(1e3 * res["ms"] / max(1, res["iterations"]), 2),
-                                                "true_rel_res": res["true_rel_res"]}
+            out[f"cg_lap2d_2048_{fmt}_{dt}"] = cg_summary(res)
+    # 3D 7-point Laplacian 160^3 (4.1M rows) and a random SPD CSR matrix
+    # (n = 1e6, power-law rows of 3..60 entries, diagonally dominant), CSR input
+    for tag, (rp, ci, v) in (("lap3d_160", M.laplacian_3d(160)), ("spd_1e6", M.random_spd(1_000_000, 7))):
+        b = np.random.default_rng(1).uniform(-1, 1, len(rp) - 1)
+        for dt in ("fp64", "mixed"):
+            x, res = P.cg_csr(rp, ci, v, b, dtype=dt, tol=1e-10)
+            out[f"cg_{tag}_csr_{dt}"] = cg_summary(res)
     return out
+
+
+def cg_summary(res):
+    return {"ms": round(res["ms"], 2), "iterations": res["iterations"],
+            "us_per_iter": round(1e3 * res["ms"] / max(1, res["iterations"]), 2),
+            "true_rel_res": res["true_rel_res"]}
 
 
 def extra_batch(P, torch, n_jobs=512, steps=100, seed=42):

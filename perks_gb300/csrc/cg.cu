@@ -60,6 +60,7 @@ struct CgMat {
   int off[kMaxDiag];
   const int* eci;         // ELL column indices [ew][n]
   int ew;
+  int grp;                // CSR: lanes per row in the SpMV phase (4, 8, 16 or 32)
 };
 
 struct CgParams {
@@ -279,20 +280,64 @@ __device__ __forceinline__ void cg_rows4(int row0, int row1, bool vec, F4&& f4, 
   for (int i = row0 + tid; i < a0; i += nt) f1(i);
   for (int i = a1 + tid; i < row1; i += nt) f1(i);
 }
-// Row-strided loop (rows i, i+nt, ...: a warp's rows are consecutive, so CSR
-// row pointers and the rows' entries stay close together), kU rows per pass.
-template <class F1>
-__device__ __forceinline__ void cg_rows1(int row0, int row1, F1&& f1) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  CG_ROWS(i, { f1(i); })
+// CSR rows by groups of G = A.grp lanes: lane l of a group takes entries
+// j0+l, j0+l+G, ... of its row, so a group reads the row's columns and values
+// as one contiguous run. Each group works on R rows per pass and steps through
+// their entries together, so up to R gathers per lane are in flight (the
+// dependent row pointer -> column -> x loads would otherwise leave the memory
+// system idle). The group adds its partial sums by shuffles and its first
+// lane runs epi(i, row sum). Every lane of the CTA runs the same number of
+// passes (the shuffles need whole warps).
+template <class XV, class MV, class XF, class Epi>
+__device__ __forceinline__ void csr_rows_grouped(const CgMat& A, const MV* __restrict__ val, int row0, int row1,
+                                                 const XF& xv, Epi&& epi) {
+  constexpr int R = 4;
+  const int G = A.grp;
+  const int gl = threadIdx.x & (G - 1);
+  const int g = threadIdx.x / G, ng = blockDim.x / G;
+  for (int i0 = row0; i0 < row1; i0 += R * ng) {
+    int j[R], j1[R];
+    XV acc[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int i = i0 + g + r * ng;
+      acc[r] = XV(0);
+      j[r] = 0;
+      j1[r] = 0;
+      if (i < row1) {
+        j[r] = __ldg(A.rp + i) + gl;
+        j1[r] = __ldg(A.rp + i + 1);
+      }
+    }
+    for (bool more = true; more;) {
+      more = false;
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        if (j[r] < j1[r]) {
+          acc[r] = fma(XV(__ldg(val + j[r])), xv(__ldg(A.ci + j[r])), acc[r]);
+          j[r] += G;
+          more |= j[r] < j1[r];
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      for (int o = G >> 1; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+      const int i = i0 + g + r * ng;
+      if (gl == 0 && i < row1) epi(i, acc[r]);
+    }
+  }
 }
-// SpMV phase rows: DIA and ELL in groups of four rows, CSR row-strided.
-template <int FMT, class F4, class F1>
-__device__ __forceinline__ void cg_rows_spmv(const CgMat& A, int row0, int row1, F4&& f4, F1&& f1) {
+
+// SpMV phase rows: DIA and ELL in groups of four rows per thread (f4; the
+// ragged ends row by row), CSR by lane groups. e1(i, row sum) finishes a row.
+template <int FMT, class XV, class MV, class XF, class F4, class E1>
+__device__ __forceinline__ void cg_rows_spmv(const CgMat& A, const MV* __restrict__ val, const XF& xv, int row0,
+                                             int row1, F4&& f4, E1&& e1) {
   if ((FMT >= 0 ? FMT : A.fmt) != 0)
-    cg_rows4(row0, row1, true, f4, f1);
+    cg_rows4(row0, row1, true, f4, [&](int i) { e1(i, spmv_row_f<XV, FMT>(A, val, xv, i)); });
   else
-    cg_rows1(row0, row1, f1);
+    csr_rows_grouped<XV>(A, val, row0, row1, xv, e1);
 }
 __device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
   const float4 t = *reinterpret_cast<const float4*>(p);
@@ -425,7 +470,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
         const T beta = r1 / r0;
         const T* __restrict__ po = static_cast<const T*>(P.p[(k + 1) & 1]);
         auto pg = [&](int c) { return fma(beta, po[c], r[c]); };
-        cg_rows_spmv<FMT>(A, row0, row1, [&](int i) {
+        cg_rows_spmv<FMT, T>(A, val, pg, row0, row1, [&](int i) {
           T av[4], pov[4], rv[4], pv[4];
           spmv4<T, FMT>(A, val, v4, pg, i, av);
           ld4(po + i, pov);
@@ -437,8 +482,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
           }
           st4(p + i, pv);
           st4(Ap + i, av);
-        }, [&](int i) {
-          const T api = spmv_row_f<T, FMT>(A, val, pg, i);
+        }, [&](int i, T api) {
           const T pi = fma(beta, po[i], r[i]);
           p[i] = pi;
           Ap[i] = api;
@@ -446,7 +490,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
         });
       } else {
         auto rg = [&](int c) { return r[c]; };
-        cg_rows_spmv<FMT>(A, row0, row1, [&](int i) {
+        cg_rows_spmv<FMT, T>(A, val, rg, row0, row1, [&](int i) {
           T av[4], rv[4];
           spmv4<T, FMT>(A, val, v4, rg, i, av);
           ld4(r + i, rv);
@@ -454,8 +498,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
           for (int u = 0; u < 4; u++) pap_t = fma(rv[u], av[u], pap_t);
           st4(p + i, rv);
           st4(Ap + i, av);
-        }, [&](int i) {
-          const T api = spmv_row_f<T, FMT>(A, val, rg, i);
+        }, [&](int i, T api) {
           const T pi = r[i];
           p[i] = pi;
           Ap[i] = api;
@@ -482,15 +525,14 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
       }
       if (!gs.gb.sync()) return;
       auto pg = [&](int c) { return p[c]; };
-      cg_rows_spmv<FMT>(A, row0, row1, [&](int i) {
+      cg_rows_spmv<FMT, T>(A, val, pg, row0, row1, [&](int i) {
         T av[4], pv[4];
         spmv4<T, FMT>(A, val, v4, pg, i, av);
         ld4(p + i, pv);
 #pragma unroll
         for (int u = 0; u < 4; u++) pap_t = fma(pv[u], av[u], pap_t);
         st4(Ap + i, av);
-      }, [&](int i) {
-        const T api = spmv_row_f<T, FMT>(A, val, pg, i);
+      }, [&](int i, T api) {
         Ap[i] = api;
         pap_t = fma(p[i], api, pap_t);
       });
@@ -595,7 +637,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       const float beta = float(rr / rr0);
       const float* __restrict__ po = static_cast<const float*>(P.p[(k + 1) & 1]);
       auto pg = [&](int c) { return fmaf(beta, po[c], r[c]); };
-      cg_rows_spmv<FMT>(A, row0, row1, [&](int i) {
+      cg_rows_spmv<FMT, float>(A, val32, pg, row0, row1, [&](int i) {
         float av[4], pov[4], rv[4], pv[4];
         spmv4<float, FMT>(A, val32, v4, pg, i, av);
         ld4(po + i, pov);
@@ -607,8 +649,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
         }
         st4(p + i, pv);
         st4(Ap + i, av);
-      }, [&](int i) {
-        const float api = spmv_row_f<float, FMT>(A, val32, pg, i);
+      }, [&](int i, float api) {
         const float pi = fmaf(beta, po[i], r[i]);
         p[i] = pi;
         Ap[i] = api;
@@ -616,7 +657,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       });
     } else {
       auto rg = [&](int c) { return r[c]; };
-      cg_rows_spmv<FMT>(A, row0, row1, [&](int i) {
+      cg_rows_spmv<FMT, float>(A, val32, rg, row0, row1, [&](int i) {
         float av[4], rv[4];
         spmv4<float, FMT>(A, val32, v4, rg, i, av);
         ld4(r + i, rv);
@@ -624,8 +665,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
         for (int u = 0; u < 4; u++) pap_t = fmaf(rv[u], av[u], pap_t);
         st4(p + i, rv);
         st4(Ap + i, av);
-      }, [&](int i) {
-        const float api = spmv_row_f<float, FMT>(A, val32, rg, i);
+      }, [&](int i, float api) {
         const float pi = r[i];
         p[i] = pi;
         Ap[i] = api;
@@ -880,6 +920,7 @@ __global__ void ell_build(const int* rp, const int* ci, const SV* val, int n, in
 constexpr int kEmpty = 0x7fffffff;
 __global__ void csr_diag_scan(const int* rp, const int* ci, int n, int* tab, int* flags) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (*((volatile int*)flags)) return;  // table full: not a DIA matrix, stop scanning
     const int j0 = rp[i], j1 = rp[i + 1];
     int prev = -1;
     for (int j = j0; j < j1; j++) {
@@ -896,7 +937,10 @@ __global__ void csr_diag_scan(const int* rp, const int* ci, int n, int* tab, int
           if (old == kEmpty || old == d) break;
         }
       }
-      if (probes == 64) flags[0] = 1;
+      if (probes == 64) {
+        flags[0] = 1;
+        return;
+      }
     }
   }
 }
@@ -1077,6 +1121,12 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
       P.A.val = mixed ? nullptr : ev;
       if (mixed) P.val32 = static_cast<float*>(ev);
     }
+  }
+  if (P.A.fmt == 0) {  // CSR SpMV: lanes per row, about half the mean row length
+    const long long avg = (A.nnz + std::max(n, 1) - 1) / std::max(n, 1);
+    int g = 4;
+    while (g < 32 && 2ll * g < avg) g *= 2;
+    P.A.grp = g;
   }
   if (mixed && P.A.fmt == A.fmt) {  // no converted copy: FP32 copy of the given values
     to_f32<<<dev->sms * 8, 256, 0, s>>>(static_cast<const double*>(A.val), nval, P.val32);

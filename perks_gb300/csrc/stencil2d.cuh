@@ -73,7 +73,7 @@ struct Geom2D {
   static constexpr bool PAIR = sizeof(T) == 4 && !BOX && SHAPE <= PERKS_2DS25PT;
 };
 
-// Warps per CTA, rows in flight and division form for one kernel: the
+// Warps per CTA, rows in flight, division form and rows per copy wait for one kernel: the
 // measured table (tune2d.cuh), else the built-in choice. The tuning tool
 // overrides all three for a whole translation unit with PERKS_TUNE_*.
 template <class T, int SHAPE, bool FAST>
@@ -94,26 +94,34 @@ struct Pick2D {
 #else
   static constexpr int FIN = FAST ? 0 : t.fin;
 #endif
+#ifdef PERKS_TUNE_RP
+  static constexpr int RP = PERKS_TUNE_RP;
+#else
+  static constexpr int RP = t.rp ? t.rp : 1;
+#endif
 };
 
 // Full configuration. The chosen values are template arguments, so kernels
 // built with different choices never share a name.
-template <class T, int SHAPE, int NW_, int D_, int FIN_>
+template <class T, int SHAPE, int NW_, int D_, int FIN_, int RP_>
 struct Cfg2DT : Geom2D<T, SHAPE> {
   using G = Geom2D<T, SHAPE>;
   static constexpr int NW = NW_;
   static constexpr int NT = NW * 32;
   static constexpr int D = D_;                           // rows in flight per warp
-  static constexpr int DR = D + 1;                       // ring slots per warp
+  static constexpr int RP = RP_;                         // rows per copy wait (1 or 2)
+  static constexpr int DR = D + RP;                      // ring slots per warp
   static constexpr int FIN = FIN_;                       // division form (divconst.cuh)
   static constexpr int SLOT = G::SW + 2 * G::H * G::V16; // ring slot: strip row + one chunk per edge lane
   static constexpr size_t ring_bytes = size_t(NW) * DR * SLOT * sizeof(T);
   static constexpr size_t res_row_bytes = size_t(NW) * G::SW * sizeof(T);  // one resident row for every warp
   static_assert(2 * G::H <= 32, "edge lanes");
   static_assert(NW >= 1 && NW <= 32 && D >= 1 && D <= 8, "launch shape");
+  static_assert(RP == 1 || (RP == 2 && D >= 2), "rows per copy wait");
 };
 template <class T, int SHAPE, bool FAST = false>
-using Cfg2D = Cfg2DT<T, SHAPE, Pick2D<T, SHAPE, FAST>::NW, Pick2D<T, SHAPE, FAST>::D, Pick2D<T, SHAPE, FAST>::FIN>;
+using Cfg2D = Cfg2DT<T, SHAPE, Pick2D<T, SHAPE, FAST>::NW, Pick2D<T, SHAPE, FAST>::D, Pick2D<T, SHAPE, FAST>::FIN,
+                    Pick2D<T, SHAPE, FAST>::RP>;
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, uint64_t pol) {
   asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(smem_u32(smem)), "l"(gmem),
@@ -341,65 +349,97 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
         qn++;
       });
 
-      auto step_rows = [&](auto fwd_c) {
+      // Compute and store output row q; j = q mod WN picks the window slots.
+      auto do_row = [&](int q, auto jc, auto fwd_c) {
+        constexpr int j = decltype(jc)::value;
         constexpr bool F = decltype(fwd_c)::value;
-        for (int q0 = 0; q0 < TY; q0 += WN) {
-          static_for<WN>([&](auto jc) {
-            constexpr int j = decltype(jc)::value;
-            const int q = q0 + j;
-            if (q < TY) {
-              cp_async_wait<D - 1>();
-              __syncwarp();
-              bring(qn, std::integral_constant<int, (j + 2 * H) % WN>{});
-              fetch(qn + D);
-              qn++;
-              const int y = F ? r0 + q : r1 - 1 - q;
-              // window slot of row y+dy
-              auto ws = [](int dy) constexpr { return (j + H + (F ? dy : -dy) + 2 * WN) % WN; };
-              WinT hc;  // star: horizontal window of the centre row
-              if constexpr (!BOX) hc = hwin(w[ws(0)]);
-              T o[V];
-              if constexpr (Cf::PAIR && !FAST) {
-                // two adjacent cells per packed FP32 instruction
+        const int y = F ? r0 + q : r1 - 1 - q;
+        // window slot of row y+dy
+        auto ws = [](int dy) constexpr { return (j + H + (F ? dy : -dy) + 2 * WN) % WN; };
+        WinT hc;  // star: horizontal window of the centre row
+        if constexpr (!BOX) hc = hwin(w[ws(0)]);
+        T o[V];
+        if constexpr (Cf::PAIR && !FAST) {
+          // two adjacent cells per packed FP32 instruction
 #pragma unroll
-                for (int i = 0; i < V; i += 2) {
-                  auto u2 = [&](int, int dy, int dx) -> F2 {
-                    if (dy == 0) return F2::pack(hc.h[H + i + dx], hc.h[H + i + 1 + dx]);
-                    return F2::pack(w[ws(dy)].v[i], w[ws(dy)].v[i + 1]);
-                  };
-                  star2d_ref<F2, SHAPE, Cf::FIN>(u2, [one2](F2 a, F2 b) { return RN<F2>::fma(b, one2, a); })
-                      .unpack(o[i], o[i + 1]);
-                }
-              } else {
+          for (int i = 0; i < V; i += 2) {
+            auto u2 = [&](int, int dy, int dx) -> F2 {
+              if (dy == 0) return F2::pack(hc.h[H + i + dx], hc.h[H + i + 1 + dx]);
+              return F2::pack(w[ws(dy)].v[i], w[ws(dy)].v[i + 1]);
+            };
+            star2d_ref<F2, SHAPE, Cf::FIN>(u2, [one2](F2 a, F2 b) { return RN<F2>::fma(b, one2, a); })
+                .unpack(o[i], o[i + 1]);
+          }
+        } else {
 #pragma unroll
-                for (int i = 0; i < V; i++) {
-                  auto u = [&](int, int dy, int dx) -> T {
-                    if constexpr (BOX) return wf[ws(dy)].h[H + i + dx];
-                    else return dy == 0 ? hc.h[H + i + dx] : w[ws(dy)].v[i];
-                  };
-                  o[i] = stencil_point<T, SHAPE, FAST, Cf::FIN>(u);
+          for (int i = 0; i < V; i++) {
+            auto u = [&](int, int dy, int dx) -> T {
+              if constexpr (BOX) return wf[ws(dy)].h[H + i + dx];
+              else return dy == 0 ? hc.h[H + i + dx] : w[ws(dy)].v[i];
+            };
+            o[i] = stencil_point<T, SHAPE, FAST, Cf::FIN>(u);
+          }
+        }
+        if (dir) {
+          const bool row_fixed = y < H || y >= wy - H;
+#pragma unroll
+          for (int i = 0; i < V; i++) {
+            const int x = xl + i;
+            T old;
+            if constexpr (BOX) old = wf[ws(0)].h[H + i];
+            else old = w[ws(0)].v[i];
+            if (row_fixed || x < H || x >= wx - H) o[i] = old;
+          }
+        }
+        T* dst = fout + size_t(y) * pitch + xl;
+        if (is_res(y)) {
+          store_lane<NV>(res_ptr(y), o);
+          if (lane * V < H || (lane + 1) * V > SW - H) store_lane<NV>(dst, o);
+        } else {
+          store_lane<NV>(dst, o);
+        }
+      };
+      auto step_rows = [&](auto fwd_c) {
+        if constexpr (Cf::RP == 1) {
+          for (int q0 = 0; q0 < TY; q0 += WN) {
+            static_for<WN>([&](auto jc) {
+              constexpr int j = decltype(jc)::value;
+              const int q = q0 + j;
+              if (q < TY) {
+                cp_async_wait<D - 1>();
+                __syncwarp();
+                bring(qn, std::integral_constant<int, (j + 2 * H) % WN>{});
+                fetch(qn + D);
+                qn++;
+                do_row(q, jc, fwd_c);
+              }
+            });
+          }
+        } else {
+          // Two rows per copy wait: one wait and one warp barrier cover both,
+          // and the two rows' arithmetic can overlap. The ring has D + 2
+          // slots, so the two slots fetched here were freed by the previous
+          // pair, before this pair's barrier.
+          for (int q0 = 0; q0 < TY; q0 += 2 * WN) {
+            static_for<WN>([&](auto pc) {
+              constexpr int j0 = 2 * decltype(pc)::value, j1 = j0 + 1;
+              const int q = q0 + j0;
+              if (q < TY) {
+                cp_async_wait<D - 2>();
+                __syncwarp();
+                bring(qn, std::integral_constant<int, (j0 + 2 * H) % WN>{});
+                fetch(qn + D);
+                fetch(qn + D + 1);
+                qn++;
+                do_row(q, std::integral_constant<int, j0 % WN>{}, fwd_c);
+                if (q + 1 < TY) {
+                  bring(qn, std::integral_constant<int, (j1 + 2 * H) % WN>{});
+                  qn++;
+                  do_row(q + 1, std::integral_constant<int, j1 % WN>{}, fwd_c);
                 }
               }
-              if (dir) {
-                const bool row_fixed = y < H || y >= wy - H;
-#pragma unroll
-                for (int i = 0; i < V; i++) {
-                  const int x = xl + i;
-                  T old;
-                  if constexpr (BOX) old = wf[ws(0)].h[H + i];
-                  else old = w[ws(0)].v[i];
-                  if (row_fixed || x < H || x >= wx - H) o[i] = old;
-                }
-              }
-              T* dst = fout + size_t(y) * pitch + xl;
-              if (is_res(y)) {
-                store_lane<NV>(res_ptr(y), o);
-                if (lane * V < H || (lane + 1) * V > SW - H) store_lane<NV>(dst, o);
-              } else {
-                store_lane<NV>(dst, o);
-              }
-            }
-          });
+            });
+          }
         }
       };
       if (fwd) step_rows(std::true_type{});

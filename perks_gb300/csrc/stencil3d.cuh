@@ -37,6 +37,7 @@
 #include "ptx.cuh"
 #include "shapes.cuh"
 #include "stencil2d.cuh"  // static_for
+#include "tune3d.cuh"
 
 namespace perks {
 
@@ -79,8 +80,40 @@ struct Stencil3DParams {
   unsigned* status;
 };
 
-template <class T, int SHAPE>
-struct Cfg3D {
+// Compute warps, rows per compute warp and the ring depth (KB of planes in
+// flight) of one kernel: the measured table (tune3d.cuh), else the built-in
+// choice. The tuning tool overrides them for a whole translation unit with
+// PERKS_TUNE3_*.
+//
+// Built-in choice, from timing FP32 variants at 512^3: the 7-point star does
+// best with 8 warps of 4 rows, the radius-2 and box shapes with 11 warps of 3
+// rows (12 warps: 168 registers per thread). FP64 is bound by the FP64 pipe:
+// 8 warps of 4 rows keep its larger windows out of local memory.
+template <class T, int SHAPE, bool FAST>
+struct Pick3D {
+  static constexpr bool WIDE = sizeof(T) == 4 && (ShapeInfo<SHAPE>::box || ShapeInfo<SHAPE>::H >= 2);
+  static constexpr Tune3D t = kTune3D[sizeof(T) == 8][FAST][SHAPE - PERKS_3D7PT];
+#ifdef PERKS_TUNE3_NWC
+  static constexpr int NWC = PERKS_TUNE3_NWC;
+#else
+  static constexpr int NWC = t.nwc ? t.nwc : WIDE ? 11 : 8;
+#endif
+#ifdef PERKS_TUNE3_RY
+  static constexpr int RY = PERKS_TUNE3_RY;
+#else
+  static constexpr int RY = t.ry ? t.ry : WIDE ? 3 : 4;
+#endif
+#ifdef PERKS_TUNE3_DKB
+  static constexpr int DKB = PERKS_TUNE3_DKB;
+#else
+  static constexpr int DKB = t.dkb ? t.dkb : 72;
+#endif
+};
+
+// Full configuration; the chosen values are template arguments, so kernels
+// built with different choices never share a name.
+template <class T, int SHAPE, int NWC_, int RY_, int DKB_>
+struct Cfg3DT {
   static constexpr int H = ShapeInfo<SHAPE>::H;
   static constexpr bool BOX = ShapeInfo<SHAPE>::box;
   static constexpr int V16 = 16 / sizeof(T);
@@ -88,14 +121,8 @@ struct Cfg3D {
   static constexpr int V = NV * V16;                      // columns per lane
   static constexpr int SW = 32 * V;                       // tile width
   static constexpr int HP = ((H + V16 - 1) / V16) * V16;  // pad columns each side (16-byte multiple)
-  // Compute warps and rows per warp (one more warp is the producer), from
-  // timing FP32 variants at 512^3: the 7-point star does best with 8 warps of
-  // 4 rows, the radius-2 and box shapes with 11 warps of 3 rows (12 warps: 168
-  // registers per thread). FP64 is bound by the FP64 pipe: 8 warps of 4 rows
-  // keep its larger windows out of local memory.
-  static constexpr bool WIDE = sizeof(T) == 4 && (BOX || H >= 2);
-  static constexpr int NWC = WIDE ? 11 : 8;
-  static constexpr int RY = WIDE ? 3 : 4;                 // rows per compute warp
+  static constexpr int NWC = NWC_;                        // compute warps (one more is the producer)
+  static constexpr int RY = RY_;                          // rows per compute warp
   static constexpr int TY = NWC * RY;                     // tile height
   static constexpr int NT = (NWC + 1) * 32;
   static constexpr int SR = TY + 2 * H;                   // slot rows
@@ -106,25 +133,26 @@ struct Cfg3D {
   static constexpr int PLANE = MAIN + 2 * PADSZ;           // slot stride (elements)
   static constexpr unsigned tx_bytes = unsigned((SR * SW + 2 * SR * HP) * sizeof(T));
   static constexpr size_t slot_bytes = size_t(PLANE) * sizeof(T);
-  // planes in flight beyond the 2H+1 being read: about 72 KB, at least 2,
-  // within a 200 KB ring
+  // planes in flight beyond the 2H+1 being read: about DKB KB, at least 2,
+  // within a 200 KB ring, and at least 1 (a ring larger than shared memory is
+  // refused by the launcher)
   static constexpr int DMAX = int((200u * 1024u) / slot_bytes) - (2 * H + 1);
-  static constexpr int DWANT = int((72u * 1024u + slot_bytes - 1) / slot_bytes) > 2
-                                   ? int((72u * 1024u + slot_bytes - 1) / slot_bytes)
+  static constexpr int DWANT = int((unsigned(DKB_) * 1024u + slot_bytes - 1) / slot_bytes) > 2
+                                   ? int((unsigned(DKB_) * 1024u + slot_bytes - 1) / slot_bytes)
                                    : 2;
-  static constexpr int D = DMAX < DWANT ? DMAX : DWANT;
+  static constexpr int D = (DMAX < DWANT ? DMAX : DWANT) < 1 ? 1 : (DMAX < DWANT ? DMAX : DWANT);
   static constexpr int NR = 2 * H + 1 + D;                // ring slots
   static constexpr size_t ring_bytes = size_t(NR) * slot_bytes;
   static constexpr size_t smem_bytes = ring_bytes + 2 * NR * sizeof(uint64_t);
-  static_assert(D >= 1, "ring too small");
+  static_assert(NWC >= 1 && NWC <= 31 && RY >= 1, "launch shape");
   static_assert(H <= V16, "horizontal neighbours are at most one lane away");
   static_assert(SW <= 256 && SR <= 256, "TMA box extent");
 };
+template <class T, int SHAPE, bool FAST = false>
+using Cfg3D = Cfg3DT<T, SHAPE, Pick3D<T, SHAPE, FAST>::NWC, Pick3D<T, SHAPE, FAST>::RY, Pick3D<T, SHAPE, FAST>::DKB>;
 
-template <class T, int SHAPE, bool FAST>
-__global__ void __launch_bounds__(Cfg3D<T, SHAPE>::NT, 1)
-    stencil3d_kernel(const __grid_constant__ Stencil3DParams p) {
-  using Cf = Cfg3D<T, SHAPE>;
+template <class T, int SHAPE, bool FAST, class Cf>
+__global__ void __launch_bounds__(Cf::NT, 1) stencil3d_kernel(const __grid_constant__ Stencil3DParams p) {
   constexpr int H = Cf::H, V = Cf::V, V16 = Cf::V16, NV = Cf::NV, SW = Cf::SW, HP = Cf::HP, RY = Cf::RY,
                 NWC = Cf::NWC, TY = Cf::TY, PLANE = Cf::PLANE, NR = Cf::NR, MAIN = Cf::MAIN, PADSZ = Cf::PADSZ;
   constexpr bool BOX = Cf::BOX;

@@ -14,7 +14,7 @@ int encode_tiled_3d(CUtensorMap* map, bool f64, void* base, int wx, int wy, int 
 template <class T, int SHAPE, bool FAST>
 int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h, int wy, int wx, int steps,
                      perks_stencil_stats* st, bool host_io = false) {
-  using Cf = Cfg3D<T, SHAPE>;
+  using Cf = Cfg3D<T, SHAPE, FAST>;
   const DeviceInfo* dev = device_info();
   if (!dev) return PERKS_ERR_NO_DEVICE;
   cudaStream_t s = static_cast<cudaStream_t>(o.stream);
@@ -77,7 +77,7 @@ int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h
   p.bar = sw.bar;
   p.status = sw.status;
 
-  auto kern = stencil3d_kernel<T, SHAPE, FAST>;
+  auto kern = stencil3d_kernel<T, SHAPE, FAST, Cf>;
   PERKS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   cudaEvent_t e0, e1;
   PERKS_CUDA(cudaEventCreate(&e0));

@@ -1,24 +1,24 @@
 // Measured launch parameters of the 2D stencil kernels on GB300, per dtype
 // (0 FP32, 1 FP64), evaluation order (0 reference, 1 fast) and 2D shape
-// (PERKS_2D5PT .. PERKS_2D25PT): warps per CTA, rows in flight per warp and
-// the division form of divconst.cuh. 0 in nw or d keeps the built-in choice
-// of stencil2d.cuh. `python -m perks_gb300.autotune` measures the candidates
+// (PERKS_2D5PT .. PERKS_2D25PT): warps per CTA, rows in flight per warp, the
+// division form of divconst.cuh and rows per copy wait. 0 in nw, d or rp
+// keeps the built-in choice of stencil2d.cuh. `python -m perks_gb300.autotune` measures the candidates
 // and rewrites the table below.
 #pragma once
 
 namespace perks {
 
 struct Tune2D {
-  int nw, d, fin;
+  int nw, d, fin, rp;  // rp 0 = one row per copy wait
 };
 
 // clang-format off
 // BEGIN TABLE
 constexpr Tune2D kTune2D[2][2][8] = {
-  {{{16, 4, 1}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}},
-   {{8, 4, 0}, {8, 6, 0}, {12, 4, 0}, {12, 6, 0}, {12, 4, 0}, {0, 0, 0}, {8, 4, 0}, {12, 4, 0}}},
-  {{{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {8, 4, 1}, {12, 6, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}},
-   {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}}}};
+  {{{16, 4, 1, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}},
+   {{8, 4, 0, 0}, {8, 6, 0, 0}, {12, 6, 0, 2}, {12, 6, 0, 0}, {12, 4, 0, 0}, {0, 0, 0, 0}, {8, 4, 0, 0}, {12, 4, 0, 0}}},
+  {{{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {8, 4, 1, 0}, {12, 6, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}},
+   {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}}}};
 // END TABLE
 // clang-format on
 

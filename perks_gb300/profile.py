@@ -41,7 +41,8 @@ def _cg(a):
     import numpy as np
     from . import cg as C
     from . import matrices as M
-    rp, ci, v = M.laplacian_2d(a.n) if a.matrix == "lap2d" else M.laplacian_3d(a.n)
+    rp, ci, v = {"lap2d": lambda: M.laplacian_2d(a.n), "lap3d": lambda: M.laplacian_3d(a.n),
+                 "spd": lambda: M.random_spd(a.n, 7)}[a.matrix]()
     b = np.random.default_rng(1).uniform(-1, 1, len(rp) - 1)
     kw = dict(dtype=a.dtype, tol=0.0, static_iter=True, check=False)
     if a.format == "dia":
@@ -77,8 +78,8 @@ def main(argv=None):
     s.add_argument("--l2-sweep", action="store_true")
     s.add_argument("--steps", type=int, default=3)
     c = sub.add_parser("cg")
-    c.add_argument("--matrix", default="lap2d", choices=["lap2d", "lap3d"])
-    c.add_argument("--n", type=int, default=512, help="grid points per dimension")
+    c.add_argument("--matrix", default="lap2d", choices=["lap2d", "lap3d", "spd"])
+    c.add_argument("--n", type=int, default=512, help="grid points per dimension (spd: rows)")
     c.add_argument("--format", default="csr", choices=["csr", "dia"])
     c.add_argument("--dtype", default="fp64", choices=["fp64", "fp32", "mixed"])
     c.add_argument("--iters", type=int, default=20)
