@@ -3,6 +3,7 @@
   python -m perks_gb300.profile stencil --shape 3d27pt --dims 256,256,256 --dtype f32 --order fast --steps 3
   python -m perks_gb300.profile cg --matrix lap2d --n 512 --dtype fp64 --iters 20
   python -m perks_gb300.profile batch --jobs 512 --steps 100
+  python -m perks_gb300.profile sweep --steps 1000     # every stencil shape, one JSON line each
 
 Runs one warm-up call, then exactly one call of the requested size, and
 prints its stats as one JSON line. The warm-up uses the same kernel with 2
@@ -35,6 +36,53 @@ def _stencil(a):
     _, st = fn(d, a.shape, a.steps, out=o, **kw)
     torch.cuda.synchronize()
     return {"shape": a.shape, "dims": dims, "dtype": a.dtype, "order": a.order, "steps": a.steps, **st}
+
+
+def _sweep(a):
+    """The stencil sweep: every shape at its sizes, FP32 and FP64 storage,
+    reference order, persistent vs one launch per step (a.steps time steps),
+    and the FP32 result's error relative to the FP64 one after a.err_steps
+    steps (the FP64 kernel is bit-identical to the CPU oracle in the tests,
+    so it stands in for the oracle at these sizes; the reference weights do
+    not sum to one, so over many steps the fields leave the floating-point
+    range and only a short run gives a meaningful error)."""
+    import torch
+    from . import stencil as S
+    cases = []
+    if "2d" in a.which:
+        cases += [(sh, (8192, 8192)) for sh in ("2d5pt", "2ds9pt", "2d13pt", "2d17pt", "2d21pt", "2ds25pt", "2d9pt",
+                                               "2d25pt")]
+    for n in (256, 512):
+        if f"3d{n}" in a.which:
+            cases += [(sh, (n, n, n)) for sh in ("3d7pt", "3d13pt", "3d17pt", "3d27pt", "poisson")]
+    rows = []
+    for shape, dims in cases:
+        fn = S.stencil2d if len(dims) == 2 else S.stencil3d
+        g = torch.Generator(device="cpu").manual_seed(1)
+        f64 = torch.rand(dims, generator=g, dtype=torch.float64)
+        res, outs = {}, {}
+        for dtn, dt in (("f32", torch.float32), ("f64", torch.float64)):
+            d = f64.to(dt).cuda()
+            o = torch.empty_like(d)
+            for kernel in ("persistent", "per_step"):
+                fn(d, shape, 2, out=o, kernel=kernel)
+                torch.cuda.synchronize()
+                _, st = fn(d, shape, a.steps, out=o, kernel=kernel)
+                torch.cuda.synchronize()
+                res[f"{dtn}_{kernel}"] = round(st["gcells_per_s"], 2)
+            fn(d, shape, a.err_steps, out=o)
+            outs[dtn] = o.double()
+            del d, o
+        diff = (outs["f32"] - outs["f64"]).abs()
+        ref = outs["f64"].abs()
+        row = {"shape": shape, "dims": list(dims), "steps": a.steps, "gcells": res, "err_steps": a.err_steps,
+               "f32_rel_max_err": float(diff.max() / ref.max()),
+               "f32_rel_rms_err": float(diff.pow(2).mean().sqrt() / outs["f64"].pow(2).mean().sqrt())}
+        del outs, diff, ref
+        torch.cuda.empty_cache()
+        print(json.dumps(row), flush=True)
+        rows.append(row)
+    return {"cases": len(rows)}
 
 
 def _cg(a):
@@ -83,6 +131,10 @@ def main(argv=None):
     c.add_argument("--format", default="csr", choices=["csr", "dia"])
     c.add_argument("--dtype", default="fp64", choices=["fp64", "fp32", "mixed"])
     c.add_argument("--iters", type=int, default=20)
+    sw = sub.add_parser("sweep")
+    sw.add_argument("--steps", type=int, default=1000)
+    sw.add_argument("--err-steps", type=int, default=10)
+    sw.add_argument("--which", default="2d,3d256,3d512", help="any of 2d, 3d256, 3d512")
     bt = sub.add_parser("batch")
     bt.add_argument("--jobs", type=int, default=512)
     bt.add_argument("--steps", type=int, default=100)
@@ -90,7 +142,7 @@ def main(argv=None):
     bt.add_argument("--threads", type=int, default=1024, help="threads per CTA (0 = autotune)")
     bt.add_argument("--ctas", type=int, default=1, help="CTAs per SM (0 = autotune)")
     a = ap.parse_args(argv)
-    out = {"stencil": _stencil, "cg": _cg, "batch": _batch}[a.what](a)
+    out = {"stencil": _stencil, "cg": _cg, "batch": _batch, "sweep": _sweep}[a.what](a)
     print(json.dumps(out, default=str), flush=True)
 
 
