@@ -147,6 +147,12 @@ def cpu_baseline(seconds_budget: float = 15.0):
             "sample": f"{SHAPE} fp32 {WY}x{WX}, {steps} time steps (of {TSTEPS}), oracle C port, OpenMP"}
 
 
+def headline_config(ws: int) -> dict:
+    return {"workload": f"{SHAPE} {DTYPE} {WY}x{WX} x{TSTEPS} time steps, persistent, reference order",
+            "shape": SHAPE, "cells": WY * WX, "time_steps_per_step": TSTEPS, "parallelism": f"replicas{ws}",
+            "l2": "inputs larger than L2 (256 MiB field)"}
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -161,11 +167,10 @@ def run_reference(args, ws, rank):
         vals.append(last["value"])
     el = time.perf_counter() - t0
     v = statistics.median(vals)
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": K,
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": K,
             "warmup": W, "ms_per_step": el * 1e3 / K, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": DTYPE, "data": "synthetic",
-            "config": {"workload": f"{SHAPE} {DTYPE} {WY}x{WX} x{TSTEPS} time steps", "shape": SHAPE,
-                       "cells": WY * WX, "time_steps": TSTEPS},
+            "vs_baseline": None, "dtype": DTYPE, "data": "synthetic (seeded uniform [0,1) field)",
+            "config": headline_config(ws), "runs_on": "host cores (rank 0), no GPU",
             "cpu_baseline": {**last, "value": v},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -312,10 +317,7 @@ def main():
                 "warmup": max(3, args.warmup), "ms_per_step": round(ms_max / args.steps, 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPE,
                 "data": "synthetic (seeded uniform [0,1) field)",
-                "config": {"workload": f"{SHAPE} {DTYPE} {WY}x{WX} x{TSTEPS} time steps, persistent, "
-                                       f"reference order", "shape": SHAPE, "cells": WY * WX,
-                           "time_steps_per_step": TSTEPS, "parallelism": f"replicas{ws}",
-                           "l2": "inputs larger than L2 (256 MiB field)"},
+                "config": headline_config(ws),
                 "e2e": {"value": round(e2e_val, 3), "unit": UNIT, "h2d_bytes_per_step": nbytes,
                         "d2h_bytes_per_step": nbytes},
                 "gpu_launches": int(launches),
