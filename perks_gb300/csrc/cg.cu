@@ -291,7 +291,7 @@ __device__ __forceinline__ void cg_rows4(int row0, int row1, bool vec, F4&& f4, 
 template <class XV, class MV, class XF, class Epi>
 __device__ __forceinline__ void csr_rows_grouped(const CgMat& A, const MV* __restrict__ val, int row0, int row1,
                                                  const XF& xv, Epi&& epi) {
-  constexpr int R = 4;
+  constexpr int R = 4;  // rows per group and pass (the reduction below is written for 4)
   const int G = A.grp;
   const int gl = threadIdx.x & (G - 1);
   const int g = threadIdx.x / G, ng = blockDim.x / G;
@@ -320,12 +320,20 @@ __device__ __forceinline__ void csr_rows_grouped(const CgMat& A, const MV* __res
         }
       }
     }
-#pragma unroll
-    for (int r = 0; r < R; r++) {
-      for (int o = G >> 1; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
-      const int i = i0 + g + r * ng;
-      if (gl == 0 && i < row1) epi(i, acc[r]);
-    }
+    // Transposing reduction of the four row sums over the group (G >= 4):
+    // the first two exchanges halve the values a lane holds, so a lane adds
+    // 2 + 1 + log2(G/4) values instead of 4 log2(G) (FP64 adds are scarce on
+    // this GPU). Afterwards lane gl < 4 holds the sum of row 2(gl&1) + (gl>>1).
+    constexpr unsigned kFull = 0xffffffffu;
+    const bool b0 = gl & 1, b1 = gl & 2;
+    const XV s0 = __shfl_xor_sync(kFull, b0 ? acc[0] : acc[2], 1);
+    const XV s1 = __shfl_xor_sync(kFull, b0 ? acc[1] : acc[3], 1);
+    const XV p0 = (b0 ? acc[2] : acc[0]) + s0;  // row 0 (or 2)
+    const XV p1 = (b0 ? acc[3] : acc[1]) + s1;  // row 1 (or 3)
+    XV t = (b1 ? p1 : p0) + __shfl_xor_sync(kFull, b1 ? p0 : p1, 2);
+    for (int o = 4; o < G; o <<= 1) t += __shfl_xor_sync(kFull, t, o);
+    const int i = i0 + g + (2 * (gl & 1) + (gl >> 1)) * ng;
+    if (gl < 4 && i < row1) epi(i, t);
   }
 }
 
@@ -414,7 +422,9 @@ __device__ __forceinline__ void spmv4(const CgMat& A, const MV* __restrict__ val
 // build rounding of the scalars r.r, p.Ap, alpha and beta).
 template <class T, int FMT>
 __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_constant__ CgParams P) {
-  constexpr bool FUSE = sizeof(T) == 4;  // p formed in the SpMV gather
+  // FP32 forms p where the SpMV gathers it, except for CSR: there the random
+  // gathers dominate, and gathering p_old and r instead of p doubles them
+  constexpr bool FUSE = sizeof(T) == 4 && FMT != 0;
   const CgMat& A = P.A;
   const T* __restrict__ val = static_cast<const T*>(A.val);
   const T* __restrict__ b = static_cast<const T*>(P.b);
@@ -611,17 +621,26 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
   const int tid = threadIdx.x, nt = blockDim.x;
   const bool v4 = A.fmt != 0 && (A.n & 3) == 0 && aligned16(A.eci);  // val32 (workspace) is aligned
 
-  // true residual in FP64 (rows split as for A: A64 has the same rows)
+  // body(i, (A64 x)_i) for every row of this CTA: CSR by lane groups, else
+  // one row per thread (rows split as for A: A64 has the same rows)
+  auto true_rows = [&](auto&& body) {
+    if constexpr (FMT64 == 0) {
+      csr_rows_grouped<double>(A64, val64, row0, row1, [&](int c) { return x[c]; }, body);
+    } else {
+      CG_ROWS(i, { body(i, spmv_row<FMT64>(A64, val64, x, i)); })
+    }
+  };
+  // true residual in FP64
   double rr = 0.0, bb = 0.0;
-  CG_ROWS(i, {
+  true_rows([&](int i, double ax) {
     const double bi = b[i];
-    const double ri = bi - spmv_row<FMT64>(A64, val64, x, i);
+    const double ri = bi - ax;
     r64[i] = ri;
     r[i] = float(ri);
     xs[i] = 0.0f;
     rr = fma(ri, ri, rr);
     bb = fma(bi, bi, bb);
-  })
+  });
   if (!gs.sum2(0, rr, bb)) return;
   const double tol2 = (P.stop == PERKS_STOP_REL) ? P.tol * P.tol * bb : P.tol * P.tol;
   double maxrr = rr, rr0 = 0.0;
@@ -633,7 +652,31 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
     // values its owner stores are the same fma)
     float* __restrict__ p = static_cast<float*>(P.p[k & 1]);
     float pap_t = 0.0f;
-    if (k > 1) {
+    if constexpr (FMT == 0) {
+      // CSR: p in its own pass (same values as the fused form), so that the
+      // SpMV gathers one vector instead of two
+      const float beta = k > 1 ? float(rr / rr0) : 0.0f;
+      const float* __restrict__ po = static_cast<const float*>(P.p[(k + 1) & 1]);
+      cg_rows4(row0, row1, true, [&](int i) {
+        float pv[4], rv[4];
+        ld4(r + i, rv);
+        if (k > 1) {
+          ld4(po + i, pv);
+#pragma unroll
+          for (int u = 0; u < 4; u++) pv[u] = fmaf(beta, pv[u], rv[u]);
+        } else {
+#pragma unroll
+          for (int u = 0; u < 4; u++) pv[u] = rv[u];
+        }
+        st4(p + i, pv);
+      }, [&](int i) { p[i] = k > 1 ? fmaf(beta, po[i], r[i]) : r[i]; });
+      if (!gs.gb.sync()) return;
+      auto pgat = [&](int c) { return p[c]; };
+      cg_rows_spmv<FMT, float>(A, val32, pgat, row0, row1, [&](int) {}, [&](int i, float api) {
+        Ap[i] = api;
+        pap_t = fmaf(p[i], api, pap_t);
+      });
+    } else if (k > 1) {
       const float beta = float(rr / rr0);
       const float* __restrict__ po = static_cast<const float*>(P.p[(k + 1) & 1]);
       auto pg = [&](int c) { return fmaf(beta, po[c], r[c]); };
@@ -713,12 +756,12 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       })
       if (!gs.gb.sync()) return;
       double rt = 0.0;
-      CG_ROWS(i, {
-        const double ri = b[i] - spmv_row<FMT64>(A64, val64, x, i);
+      true_rows([&](int i, double ax) {
+        const double ri = b[i] - ax;
         r64[i] = ri;
         r[i] = float(ri);
         rt = fma(ri, ri, rt);
-      })
+      });
       if (!gs.sum1(0, rt)) return;
       rrn = rt;
       maxrr = rt;
@@ -1122,11 +1165,12 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
       if (mixed) P.val32 = static_cast<float*>(ev);
     }
   }
-  if (P.A.fmt == 0) {  // CSR SpMV: lanes per row, about half the mean row length
+  if (A.fmt == 0) {  // CSR SpMV: lanes per row, about half the mean row length
     const long long avg = (A.nnz + std::max(n, 1) - 1) / std::max(n, 1);
     int g = 4;
     while (g < 32 && 2ll * g < avg) g *= 2;
-    P.A.grp = g;
+    P.A64.grp = g;  // the FP64 true residual of mixed precision uses the matrix as given
+    if (P.A.fmt == 0) P.A.grp = g;
   }
   if (mixed && P.A.fmt == A.fmt) {  // no converted copy: FP32 copy of the given values
     to_f32<<<dev->sms * 8, 256, 0, s>>>(static_cast<const double*>(A.val), nval, P.val32);
@@ -1134,9 +1178,12 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
     count_launch(1);
   }
 
-  // the iterate's p: FP32 persistent iterations alternate two buffers
-  // (iteration k writes P.p[k & 1]); the others keep p in P.p[0]
-  auto p_of = [&](int k) { return (f32 && o->kernel == PERKS_KERNEL_PERSISTENT) ? P.p[k & 1] : P.p[0]; };
+  // the iterate's p: FP32 persistent iterations that form p in the gather
+  // (DIA, ELL) alternate two buffers (iteration k writes P.p[k & 1]); the
+  // others keep p in P.p[0]
+  auto p_of = [&](int k) {
+    return (f32 && o->kernel == PERKS_KERNEL_PERSISTENT && P.A.fmt != 0) ? P.p[k & 1] : P.p[0];
+  };
   if (resume) {
     PERKS_CUDA(cudaMemcpyAsync(P.r, ck->d_r, size_t(n) * ws, cudaMemcpyDeviceToDevice, s));
     PERKS_CUDA(cudaMemcpyAsync(p_of(ck->k), ck->d_p, size_t(n) * ws, cudaMemcpyDeviceToDevice, s));
