@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define PERKS_ABI_VERSION 2
+#define PERKS_ABI_VERSION 3
 
 /* ------------------------------------------------------------------ codes */
 typedef enum {
@@ -127,9 +127,11 @@ PERKS_API int perks_stencil3d(const perks_stencil_opts* opts, const void* d_in, 
  * perks_stencil2d (reference evaluation order only), but all scratch comes
  * from one 32 MiB static device array inside the library: fields needing more
  * (2 * width_y * padded width * sizeof(REAL) + 256 bytes) are rejected with
- * PERKS_ERR_INVALID_ARG. The first call on a device resolves the array's
- * address and should come before any stream capture. Calls share the array:
- * calls whose GPU work overlaps race and must not be issued. */
+ * PERKS_ERR_INVALID_ARG. Every call looks up the array's address on the
+ * current device (no allocation); the first call on a device may load the
+ * library's device code and should come before any stream capture. Calls
+ * share the array: calls whose GPU work overlaps race and must not be
+ * issued. */
 PERKS_API int perks_stencil2d_noalloc(const perks_stencil_opts* opts, const void* d_in, void* d_out,
                                       int width_y, int width_x, int steps, perks_stencil_stats* stats);
 
@@ -195,6 +197,8 @@ typedef struct {
   double bb;        /* b.b (relative stop) */
   int k;            /* iterations completed; 0 = no state yet (start from x) */
   int kernel;       /* perks_kernel that wrote the state; resuming needs the same */
+  int dtype;        /* perks_dtype that wrote the state; resuming needs the same */
+  int n;            /* rows of the solve that wrote it; resuming needs the same */
 } perks_cg_state;
 
 typedef struct {
@@ -336,6 +340,23 @@ PERKS_API int perks_mtx_read_csr(const char* path, int rows, long long nnz_cap, 
 PERKS_API const char* perks_last_error(void);     /* thread-local message of the last failure */
 PERKS_API const char* perks_status_string(int status);
 PERKS_API int perks_abi_version(void);
+/* Testing hook for the device-side timeout path (no counterpart in the
+ * reference). Every device-side wait of the persistent kernels (grid barrier,
+ * batch job barrier, bulk-copy mbarrier) gives up after a clock budget, sets
+ * the kernel's status word and leaves; the call then returns
+ * PERKS_ERR_TIMEOUT and the CUDA context stays usable. This sets, for the
+ * launches that follow in this process, the budget in SM clock cycles
+ * (<= 0: the default, about 2^32) and a CTA index that skips its first
+ * grid-barrier arrival (batch plans: the slice index that skips its first job
+ * barrier), so that every waiting CTA's budget runs out (< 0: none). Batch
+ * plans take the setting when they are created. Returns PERKS_OK. */
+PERKS_API int perks_debug_set_wait_fault(long long budget_cycles, int skip_cta);
+
+/* Device allocations (cudaMalloc) the library's own grow-only workspace has
+ * made in this process: lets a test check that an entry point allocated
+ * nothing. */
+PERKS_API long long perks_debug_workspace_allocs(void);
+
 /* Kernels launched by this thread since the counter was last reset. */
 PERKS_API long long perks_launch_count(void);
 PERKS_API void perks_reset_launch_count(void);

@@ -32,10 +32,25 @@ _I = ctypes.c_int
 _D = ctypes.c_double
 
 
+def reference_dir() -> str | None:
+    """The reference checkout whose CPU code builds _ref: $PERKS_REFERENCE_DIR,
+    else a checkout named ``reference`` beside this repository; None when
+    neither holds the reference's sources."""
+    for d in (os.environ.get("PERKS_REFERENCE_DIR"),
+              os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")):
+        if d and os.path.exists(os.path.join(d, "stencil", "2dstencil", "2d5pt", "jacobi_gold_gen.cpp")):
+            return os.path.abspath(d)
+    return None
+
+
 def build(quiet: bool = True) -> None:
     """Run the oracle Makefile (the restatement always; _ref when the
-    reference sources exist on this machine)."""
-    out = subprocess.run(["make", "-C", HERE, "-j8"], capture_output=True, text=True)
+    reference sources are found, see reference_dir)."""
+    cmd = ["make", "-C", HERE, "-j8"]
+    ref = reference_dir()
+    if ref:
+        cmd.append("REF=" + ref)
+    out = subprocess.run(cmd, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     if not quiet:

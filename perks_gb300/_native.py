@@ -47,7 +47,7 @@ class StencilStats(ctypes.Structure):
 
 class CgState(ctypes.Structure):
     _fields_ = [("d_r", c_void_p), ("d_p", c_void_p), ("rr", c_double), ("rr_prev", c_double),
-                ("bb", c_double), ("k", c_int), ("kernel", c_int)]
+                ("bb", c_double), ("k", c_int), ("kernel", c_int), ("dtype", c_int), ("n", c_int)]
 
 
 class CgOpts(ctypes.Structure):
@@ -119,12 +119,14 @@ SIGNATURES = {
     "perks_last_error": (ctypes.c_char_p, []),
     "perks_status_string": (ctypes.c_char_p, [c_int]),
     "perks_abi_version": (c_int, []),
+    "perks_debug_set_wait_fault": (c_int, [ctypes.c_longlong, c_int]),
+    "perks_debug_workspace_allocs": (ctypes.c_longlong, []),
     "perks_launch_count": (ctypes.c_longlong, []),
     "perks_reset_launch_count": (None, []),
 }
 
 _lib = None
-ABI_VERSION = 2  # PERKS_ABI_VERSION of include/perks.h that the structures above follow
+ABI_VERSION = 3  # PERKS_ABI_VERSION of include/perks.h that the structures above follow
 
 
 class PerksError(RuntimeError):

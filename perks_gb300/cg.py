@@ -55,7 +55,7 @@ class CgCheckpoint:
     def to_host(self) -> dict:
         st = self.state
         return {"r": self.r.cpu().numpy(), "p": self.p.cpu().numpy(), "rr": st.rr, "rr_prev": st.rr_prev,
-                "bb": st.bb, "k": st.k, "kernel": st.kernel}
+                "bb": st.bb, "k": st.k, "kernel": st.kernel, "dtype": st.dtype, "n": st.n}
 
     @classmethod
     def from_host(cls, d: dict, device="cuda") -> "CgCheckpoint":
@@ -67,6 +67,8 @@ class CgCheckpoint:
             setattr(c.state, f, float(d[f]))
         c.state.k = int(d["k"])
         c.state.kernel = int(d["kernel"])
+        c.state.dtype = int(d["dtype"])
+        c.state.n = int(d["n"])
         return c
 
 

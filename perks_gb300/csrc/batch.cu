@@ -55,18 +55,20 @@ struct BItem {  // one work item: a job, or one row slice of a stencil job
 };
 
 // Barrier of the nslices CTAs working on one job: monotonic counter, target
-// = (steps done) x nslices. False when the wait ran out its budget.
-__device__ __forceinline__ bool job_barrier(unsigned* bar, unsigned target) {
+// = (steps done) x nslices. False when the wait ran out its budget. `skip`
+// (test hook, WaitCtl::skip_cta): this CTA does not arrive, so the wait of
+// every slice of the job runs out.
+__device__ __forceinline__ bool job_barrier(unsigned* bar, unsigned target, long long budget, bool skip) {
   __shared__ unsigned s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    unsigned ok = 1, old;
+    unsigned ok = 1, old = 0u;
     __threadfence();
-    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(bar) : "memory");
-    if (int(old + 1u - target) < 0) {
+    if (!skip) asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(bar) : "memory");
+    if (skip || int(old + 1u - target) < 0) {
       const long long t0 = clock64();
       while (int(ld_acquire_gpu(bar) - target) < 0) {
-        if (clock64() - t0 > kWaitBudget) {
+        if (clock64() - t0 > budget) {
           ok = 0;
           break;
         }
@@ -120,7 +122,7 @@ __device__ __forceinline__ void stencil_rows(const BJob& J, const T* __restrict_
 
 // A stencil job cut into nslices row slices, this CTA holding one of them.
 template <class T, int SHAPE>
-__device__ void batch_stencil_slice(const BJob& J, const BItem& I, unsigned* bar, BRes* res) {
+__device__ void batch_stencil_slice(const BJob& J, const BItem& I, unsigned* bar, BRes* res, const WaitCtl& ctl) {
   const int steps = J.steps;
   const T* src = static_cast<const T*>(J.in);
   T* out = static_cast<T*>(J.out);
@@ -129,7 +131,7 @@ __device__ void batch_stencil_slice(const BJob& J, const BItem& I, unsigned* bar
   for (int t = 0; t < steps; t++) {
     T* dst = ((steps - 1 - t) & 1) == 0 ? out : scratch;  // the last step writes `out`
     stencil_rows<T, SHAPE, true>(J, src, dst, I.row_lo, I.row_hi);
-    if (!job_barrier(bar, unsigned(t + 1) * unsigned(I.nslices))) break;
+    if (!job_barrier(bar, unsigned(t + 1) * unsigned(I.nslices), ctl.budget, t == 0 && I.slice == ctl.skip_cta)) break;
     src = dst;
     done = t + 1;
   }
@@ -242,7 +244,7 @@ __device__ void batch_cg(const BJob& J, double* red, BRes* res) {
 // counter[0]: the queue; counter[1 + job]: the job barriers (all zero at launch)
 __global__ void __launch_bounds__(1024, 1)
     batch_kernel(const BJob* __restrict__ jobs, const BItem* __restrict__ items, int nitems, BRes* res,
-                 unsigned* counter, unsigned smem_bytes) {
+                 unsigned* counter, unsigned smem_bytes, const WaitCtl ctl) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int sq;
   __shared__ double red[32];
@@ -259,20 +261,20 @@ __global__ void __launch_bounds__(1024, 1)
       unsigned* bar = counter + 1 + j;
       switch (J.shape) {
         case PERKS_2D5PT:
-          if (f64) batch_stencil_slice<double, PERKS_2D5PT>(J, I, bar, res + j);
-          else batch_stencil_slice<float, PERKS_2D5PT>(J, I, bar, res + j);
+          if (f64) batch_stencil_slice<double, PERKS_2D5PT>(J, I, bar, res + j, ctl);
+          else batch_stencil_slice<float, PERKS_2D5PT>(J, I, bar, res + j, ctl);
           break;
         case PERKS_2DS9PT:
-          if (f64) batch_stencil_slice<double, PERKS_2DS9PT>(J, I, bar, res + j);
-          else batch_stencil_slice<float, PERKS_2DS9PT>(J, I, bar, res + j);
+          if (f64) batch_stencil_slice<double, PERKS_2DS9PT>(J, I, bar, res + j, ctl);
+          else batch_stencil_slice<float, PERKS_2DS9PT>(J, I, bar, res + j, ctl);
           break;
         case PERKS_2D9PT:
-          if (f64) batch_stencil_slice<double, PERKS_2D9PT>(J, I, bar, res + j);
-          else batch_stencil_slice<float, PERKS_2D9PT>(J, I, bar, res + j);
+          if (f64) batch_stencil_slice<double, PERKS_2D9PT>(J, I, bar, res + j, ctl);
+          else batch_stencil_slice<float, PERKS_2D9PT>(J, I, bar, res + j, ctl);
           break;
         default:
-          if (f64) batch_stencil_slice<double, PERKS_3D7PT>(J, I, bar, res + j);
-          else batch_stencil_slice<float, PERKS_3D7PT>(J, I, bar, res + j);
+          if (f64) batch_stencil_slice<double, PERKS_3D7PT>(J, I, bar, res + j, ctl);
+          else batch_stencil_slice<float, PERKS_3D7PT>(J, I, bar, res + j, ctl);
           break;
       }
     } else if (J.kind == PERKS_JOB_CG) {
@@ -324,6 +326,7 @@ struct perks_batch_plan_s {
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   float last_ms = 0.f;
+  WaitCtl ctl;  // wait budget of the plan's launches (taken when the plan is made)
 };
 
 namespace {
@@ -358,7 +361,8 @@ int launch_once(perks_batch_plan p, cudaStream_t s, int threads, int ctas, unsig
   const int grid = device_info()->sms * ctas;
   PERKS_CUDA(cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned) * (1 + p->njobs), s));
   PERKS_CUDA(cudaEventRecord(p->e0, s));
-  batch_kernel<<<grid, threads, smem, s>>>(p->d_jobs, p->d_items, p->nitems, p->d_res, p->d_counter, smem);
+  batch_kernel<<<grid, threads, smem, s>>>(p->d_jobs, p->d_items, p->nitems, p->d_res, p->d_counter, smem,
+                                           p->ctl);
   PERKS_CUDA(cudaGetLastError());
   PERKS_CUDA(cudaEventRecord(p->e1, s));
   PERKS_CUDA(cudaEventSynchronize(p->e1));
@@ -418,6 +422,7 @@ int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_
     }
   }
   perks_batch_plan p = new perks_batch_plan_s();
+  p->ctl = wait_ctl();
   p->device = dev->device;
   p->stream = static_cast<cudaStream_t>(o.stream);
   p->njobs = njobs;
@@ -568,7 +573,7 @@ int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_
   if (e == cudaSuccess) {
     cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned) * (1 + p->njobs), cs);
     batch_kernel<<<p->grid, p->threads, p->smem, cs>>>(p->d_jobs, p->d_items, p->nitems, p->d_res, p->d_counter,
-                                                       p->smem);
+                                                       p->smem, p->ctl);
     e = cudaStreamEndCapture(cs, &p->graph);
   }
   cudaStreamDestroy(cs);

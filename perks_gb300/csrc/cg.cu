@@ -87,6 +87,7 @@ struct CgParams {
   double rr0, rrp0, bb0;
   unsigned* bar;
   unsigned* status;
+  WaitCtl ctl;
 };
 
 // Merge-path split: first row of CTA `c` such that row + row_ptr[row] >= c*(n+nnz)/ncta.
@@ -433,7 +434,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
   T* __restrict__ Ap = static_cast<T*>(P.Ap);
   const int G = gridDim.x;
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
-  GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G)}};
+  GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G), P.ctl}};
   const int tid = threadIdx.x, nt = blockDim.x;
   const bool xvec = aligned16(x);  // the caller's solution vector
   const bool v4 = A.fmt != 0 && (A.n & 3) == 0 && aligned16(val) && aligned16(A.eci);  // DIA/ELL columns 16-byte aligned
@@ -617,7 +618,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
   float* __restrict__ xs = P.xs;
   const int G = gridDim.x;
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
-  GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G)}};
+  GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G), P.ctl}};
   const int tid = threadIdx.x, nt = blockDim.x;
   const bool v4 = A.fmt != 0 && (A.n & 3) == 0 && aligned16(A.eci);  // val32 (workspace) is aligned
 
@@ -1022,6 +1023,13 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
     if (!ck->d_r || !ck->d_p || ck->k < 0) return fail(PERKS_ERR_INVALID_ARG, "bad checkpoint");
     if (ck->k > 0 && ck->kernel != o->kernel)
       return fail(PERKS_ERR_INVALID_ARG, "checkpoint was written by the other kernel kind");
+    // d_r and d_p hold n elements of the writer's working type: a different
+    // dtype or size would read and write them out of bounds
+    if (ck->k > 0 && ck->dtype != o->dtype)
+      return fail(PERKS_ERR_INVALID_ARG, "checkpoint was written by a solve of another dtype");
+    if (ck->k > 0 && ck->n != A.n)
+      return fail(PERKS_ERR_INVALID_ARG, "checkpoint was written by a solve of " + std::to_string(ck->n) +
+                                             " rows, this one has " + std::to_string(A.n));
   }
   const bool resume = ck && ck->k > 0;
   const DeviceInfo* dev = device_info();
@@ -1077,6 +1085,7 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   }
   P.bar = sw.bar;
   P.status = sw.status;
+  P.ctl = wait_ctl();
   PERKS_CUDA(cudaMemsetAsync(scal, 0, 32 * sizeof(double), s));
 
   // The timed region includes the matrix setup below.
@@ -1288,6 +1297,8 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
     ck->bb = bbs;
     ck->k = iters;
     ck->kernel = o->kernel;
+    ck->dtype = o->dtype;
+    ck->n = n;
   }
   // true relative residual in FP64
   double* tpart = P.part;

@@ -17,8 +17,11 @@
 //    rounded up to the kernel's column-strip width; larger fields are
 //    rejected with PERKS_ERR_INVALID_ARG and a message giving both sizes.
 //    Every GPU that loads the library holds the array until the process exits.
-//  * The first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current) and caches it; make that
+//  * Every call looks up the array's device address on the current device
+//    with cudaGetSymbolAddress (a lookup; it allocates nothing), so a device
+//    reset between two calls, after which the library's device code is loaded
+//    again and the array may sit elsewhere, cannot leave a stale address. The
+//    first call on a device may load the library's device code: make that
 //    first call before any stream capture.
 //  * All calls share the one array and it keeps the last call's contents. The
 //    barrier and status words are cleared at the start of every call; the
@@ -31,7 +34,6 @@
 //    rejected with PERKS_ERR_UNSUPPORTED.
 #include <cuda_runtime.h>
 #include <algorithm>
-#include <mutex>
 #include <string>
 #include "runtime.cuh"
 #include "stencil2d_host.cuh"
@@ -42,22 +44,14 @@ constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-static std::mutex g_noalloc_mu;
-static void* g_noalloc_ptr[64] = {};
-
-// Device address of the scratch array on the current device (set up once).
+// Device address of the scratch array on the current device. In host code
+// g_noalloc_scratch names a host-side stand-in, not device memory: only this
+// looked-up address may be passed to copies and kernels.
 static int noalloc_scratch(void** out) {
-  int dev = 0;
-  PERKS_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return fail(PERKS_ERR_UNSUPPORTED, "device index out of range");
-  std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
+  *out = p;
   return PERKS_OK;
 }
 
@@ -87,6 +81,7 @@ static int noalloc2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   int C = 0;
   if (steps > 1) C = std::max(0, std::min(max_cache_rows<Cf>(o, *dev), tymax - 2 * H));
   const size_t smem = Cf::ring_bytes + size_t(C) * Cf::res_row_bytes;
+  if (smem > dev->smem_optin) return fail(PERKS_ERR_UNSUPPORTED, "shared memory budget exceeded");
   if (st) {
     *st = perks_stencil_stats{};
     st->grid_x = ns;
@@ -126,6 +121,7 @@ static int noalloc2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   p.persistent = persistent;
   p.bar = words;
   p.status = words + 2;
+  p.ctl = wait_ctl();
   auto kern = stencil2d_kernel<T, SHAPE, FAST, Cf>;
   PERKS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   if (persistent) {

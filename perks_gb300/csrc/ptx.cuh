@@ -19,8 +19,19 @@ enum : unsigned {
   kErrNonFinite = 1u << 4,        // CG: non-finite residual
 };
 
-// About 2^32 clocks (~2 s at 2 GHz): far above any legitimate wait.
+// Default budget of every device-side wait: about 2^32 clocks (~2 s at
+// 2 GHz), far above any legitimate wait. Kernels take the budget as a launch
+// parameter (WaitCtl below), so a test can shorten it.
 constexpr long long kWaitBudget = 1ll << 32;
+
+// Wait budget and the test hook that makes one CTA skip its first grid-barrier
+// arrival (so that every other CTA's bounded wait runs out). Filled on the
+// host from the process-wide settings (perks_debug_set_wait_fault); in normal
+// use budget = kWaitBudget and skip_cta = -1.
+struct WaitCtl {
+  long long budget = kWaitBudget;
+  int skip_cta = -1;
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -57,11 +68,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   return ok != 0;
 }
 // Bounded wait for phase `parity` of `bar`. Returns false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, long long budget) {
   if (mbar_try_wait(bar, parity)) return true;
   long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitBudget) return false;
+    if (clock64() - t0 > budget) return false;
   }
   return true;
 }
@@ -149,6 +160,7 @@ struct GridBarrier {
   unsigned* bar;
   unsigned* status;
   unsigned nblocks;
+  WaitCtl ctl;
   unsigned epoch = 0;  // barriers passed by this CTA (identical in every thread)
 
   __device__ __forceinline__ bool sync() {
@@ -163,14 +175,21 @@ struct GridBarrier {
       // __syncthreads); acq_rel makes the last arriver, which does not spin,
       // acquire the other CTAs' writes too (L1 may hold stale lines otherwise).
       __threadfence();
-      asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(bar) : "memory");
-      if (int(old + 1u - target) < 0) {
+      bool skip = epoch == 1 && int(blockIdx.x) == ctl.skip_cta;
+      if (skip) {
+        // test hook: this CTA does not arrive, so at most nblocks - 1 arrivals
+        // come and every CTA's wait (its own included) runs out its budget
+        old = 0u;
+      } else {
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(bar) : "memory");
+      }
+      if (skip || int(old + 1u - target) < 0) {
         long long t0 = clock64();
         unsigned spins = 0;
         while (int(ld_acquire_gpu(bar) - target) < 0) {
           if ((++spins & 63u) == 0u) {
             if (*((volatile unsigned*)status) != 0u) { ok = 0; break; }
-            if (clock64() - t0 > kWaitBudget) {
+            if (clock64() - t0 > ctl.budget) {
               atomicOr(status, kErrBarrierTimeout);
               ok = 0;
               break;

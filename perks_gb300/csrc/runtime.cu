@@ -9,6 +9,7 @@ namespace perks {
 
 static thread_local std::string g_last_error;
 static thread_local long long g_launches = 0;
+static long long g_ws_allocs = 0;  // cudaMalloc calls made by workspace() (guarded by g_mu)
 
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -83,6 +84,7 @@ void* workspace(WorkSlot slot, size_t bytes, int* status) {
       w.bytes = 0;
     }
     size_t sz = (bytes + 255) & ~size_t(255);
+    g_ws_allocs++;
     e = cudaMalloc(&w.ptr, sz);
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -100,6 +102,18 @@ void* workspace(WorkSlot slot, size_t bytes, int* status) {
 }
 
 void count_launch(int n) { g_launches += n; }
+
+static WaitCtl g_wait_ctl;
+WaitCtl wait_ctl() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return g_wait_ctl;
+}
+int set_wait_ctl(long long budget, int skip_cta) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_wait_ctl.budget = budget > 0 ? budget : kWaitBudget;
+  g_wait_ctl.skip_cta = skip_cta >= 0 ? skip_cta : -1;
+  return PERKS_OK;
+}
 
 int sync_words(SyncWords* out, cudaStream_t s) {
   int st = PERKS_OK;
@@ -146,6 +160,13 @@ const char* perks_status_string(int status) {
 }
 
 int perks_abi_version(void) { return PERKS_ABI_VERSION; }
+long long perks_debug_workspace_allocs(void) {
+  std::lock_guard<std::mutex> lk(perks::g_mu);
+  return perks::g_ws_allocs;
+}
+int perks_debug_set_wait_fault(long long budget_cycles, int skip_cta) {
+  return perks::set_wait_ctl(budget_cycles, skip_cta);
+}
 long long perks_launch_count(void) { return perks::g_launches; }
 void perks_reset_launch_count(void) { perks::g_launches = 0; }
 

@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <string>
 #include "../../include/perks.h"
+#include "ptx.cuh"
 
 namespace perks {
 
@@ -35,6 +36,10 @@ enum WorkSlot { kWsField0 = 0, kWsField1, kWsSync, kWsCgVec, kWsCgScalar, kWsCgM
 void* workspace(WorkSlot slot, size_t bytes, int* status);
 
 void count_launch(int n = 1);
+
+// Wait budget and grid-barrier test hook for the next launches (process-wide;
+// set by perks_debug_set_wait_fault, default: kWaitBudget, no hook).
+WaitCtl wait_ctl();
 
 // rows x width bytes between pitched buffers; one linear copy when both
 // pitches equal the width (a pitched copy of a dense field moves rows one

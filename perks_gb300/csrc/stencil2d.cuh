@@ -45,6 +45,7 @@ struct Stencil2DParams {
   int dirichlet, alternate, persistent;
   unsigned* bar;     // grid barrier words [2]
   unsigned* status;  // error word
+  WaitCtl ctl;       // wait budget (and the test hook of the grid barrier)
   float one = 1.0f;  // 1.0 the compiler cannot see (packed FP32 sums, see f32x2.cuh)
 };
 
@@ -234,7 +235,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
     use_in_r[d - 1] = (31 - lane) * V >= d;
   }
 
-  GridBarrier gbar{p.bar, p.status, gridDim.x};
+  GridBarrier gbar{p.bar, p.status, gridDim.x, p.ctl};
   const uint64_t pol = policy_evict_normal();
   const uint64_t pol_first = policy_evict_first();
   const F2 one2(p.one);

@@ -112,6 +112,7 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   p.persistent = persistent;
   p.bar = sw.bar;
   p.status = sw.status;
+  p.ctl = wait_ctl();
 
   auto kern = stencil2d_kernel<T, SHAPE, FAST, Cf>;
   PERKS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));

@@ -78,6 +78,7 @@ struct Stencil3DParams {
   int dirichlet, alternate, persistent;
   unsigned* bar;
   unsigned* status;
+  WaitCtl ctl;  // wait budget (and the test hook of the grid barrier)
 };
 
 // Compute warps, rows per compute warp and the ring depth (KB of planes in
@@ -181,7 +182,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil3d_kernel(const __grid_const
   }
   __syncthreads();
 
-  GridBarrier gbar{p.bar, p.status, gridDim.x};
+  GridBarrier gbar{p.bar, p.status, gridDim.x, p.ctl};
   const uint64_t pol = policy_evict_normal();
   bool ok = true;
   // Positions: every plane a CTA loads gets the next global position P; its
@@ -213,7 +214,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil3d_kernel(const __grid_const
         for (int q = -H; q < ZN + H; q++) {
           const int s = slot_index(q);
           if (pc + H + q >= NR) {  // wait until every compute warp released the slot's previous plane
-            bool w = mbar_wait(&empty[s], slot_parity(q) ^ 1u);
+            bool w = mbar_wait(&empty[s], slot_parity(q) ^ 1u, p.ctl.budget);
             w = __all_sync(0xffffffffu, w);
             if (!w) {
               if (lane == 0) atomicOr(p.status, kErrCopyTimeout);
@@ -313,7 +314,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil3d_kernel(const __grid_const
         int wq = -H;  // next segment position to wait for
         for (int q = 0; q < ZN && ok; q++) {
           for (; wq <= q + H; wq++) {
-            bool w = mbar_wait(&full[slot_index(wq)], slot_parity(wq));
+            bool w = mbar_wait(&full[slot_index(wq)], slot_parity(wq), p.ctl.budget);
             w = __all_sync(0xffffffffu, w);
             if (!w) {
               if (lane == 0) atomicOr(p.status, kErrCopyTimeout);
@@ -426,6 +427,8 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil3d_kernel(const __grid_const
   if (!ok && producer && lane == 0) {
     // leave no bulk copy in flight into this CTA's shared memory: the last NR
     // issued positions are the only ones whose copies may still be running
+    // (a budget of its own, independent of p.ctl: copies end by themselves,
+    // and a shortened test budget must not cut this wait short)
     for (long long P = max(0ll, issued - NR); P < issued; P++) {
       const int s = int(P % NR);
       const unsigned par = unsigned((P / NR) & 1);

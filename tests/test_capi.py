@@ -43,10 +43,10 @@ def test_struct_layout_matches_c(native):
 #include <stddef.h>
 #include "perks.h"
 int main(void) {
-  printf("%zu %zu %zu %zu\n", sizeof(perks_stencil_opts), sizeof(perks_stencil_stats),
-         sizeof(perks_cg_opts), sizeof(perks_cg_result));
-  printf("%zu %zu %zu\n", offsetof(perks_stencil_opts, stream), offsetof(perks_cg_opts, stream),
-         offsetof(perks_cg_result, launches));
+  printf("%zu %zu %zu %zu %zu\n", sizeof(perks_stencil_opts), sizeof(perks_stencil_stats),
+         sizeof(perks_cg_opts), sizeof(perks_cg_result), sizeof(perks_cg_state));
+  printf("%zu %zu %zu %zu\n", offsetof(perks_stencil_opts, stream), offsetof(perks_cg_opts, stream),
+         offsetof(perks_cg_result, launches), offsetof(perks_cg_state, n));
   return 0;
 }'''
     with tempfile.TemporaryDirectory() as d:
@@ -58,8 +58,9 @@ int main(void) {
     sizes = [int(x) for x in lines[0].split()]
     offs = [int(x) for x in lines[1].split()]
     assert sizes == [ctypes.sizeof(N.StencilOpts), ctypes.sizeof(N.StencilStats), ctypes.sizeof(N.CgOpts),
-                     ctypes.sizeof(N.CgResult)]
-    assert offs == [N.StencilOpts.stream.offset, N.CgOpts.stream.offset, N.CgResult.launches.offset]
+                     ctypes.sizeof(N.CgResult), ctypes.sizeof(N.CgState)]
+    assert offs == [N.StencilOpts.stream.offset, N.CgOpts.stream.offset, N.CgResult.launches.offset,
+                    N.CgState.n.offset]
 
 
 def test_enum_values_match_header(native):
@@ -73,7 +74,7 @@ def test_enum_values_match_header(native):
 
 def test_status_strings_and_version(native):
     L = native.lib()
-    assert L.perks_abi_version() == 2
+    assert L.perks_abi_version() == native._native.ABI_VERSION == 3
     assert L.perks_status_string(0) == b"ok"
     assert L.perks_status_string(-15) == b"device-side wait timed out"
 
@@ -115,3 +116,27 @@ def test_no_device_is_reported(native):
     rc = native.jacobi_iterative(a, 8, 8, b, iteration=1)
     assert rc in (-12, -13)
     assert native.last_error()
+
+
+def test_checkpoint_of_another_solve_rejected_before_launch(native):
+    """A checkpoint holds n elements of the writer's working type in d_r and
+    d_p: resuming it with another dtype or size is refused by the argument
+    checks, before any device access (the pointers here are never used)."""
+    L = native.lib()
+    N = native._native
+    st = N.CgState()
+    st.d_r, st.d_p, st.k, st.kernel = 16, 16, 5, N.KERNEL_PERSISTENT
+    st.dtype, st.n = N.FP32, 10
+    o = N.CgOpts()
+    L.perks_cg_default_opts(ctypes.byref(o))
+    o.checkpoint = ctypes.pointer(st)
+    fake = ctypes.c_void_p(16)
+    res = N.CgResult()
+    o.dtype = N.FP64  # FP32 state, FP64 solve
+    assert L.perks_cg_csr(10, 28, fake, fake, fake, fake, fake, ctypes.byref(o), ctypes.byref(res)) == -10
+    assert b"another dtype" in L.perks_last_error()
+    o.dtype = N.FP32
+    assert L.perks_cg_csr(12, 34, fake, fake, fake, fake, fake, ctypes.byref(o), ctypes.byref(res)) == -10
+    assert b"rows" in L.perks_last_error()
+    st.kernel = N.KERNEL_PER_STEP  # written by the other kernel kind
+    assert L.perks_cg_csr(10, 28, fake, fake, fake, fake, fake, ctypes.byref(o), ctypes.byref(res)) == -10

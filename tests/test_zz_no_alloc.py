@@ -15,11 +15,11 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _call(native, fn, field, shape, steps, **kw):
+def _call(native, fn, field, shape, steps, out=None, **kw):
     import torch
     from perks_gb300 import _native as N
     from perks_gb300.stencil import _opts, _torch_dtype_np
-    out = torch.empty_like(field)
+    out = torch.empty_like(field) if out is None else out
     o = _opts(shape, _torch_dtype_np(field), stream=ctypes.c_void_p(torch.cuda.current_stream().cuda_stream),
               **kw)
     st = N.StencilStats()
@@ -52,3 +52,31 @@ def test_noalloc_rejects_oversized_field(native, cuda):
     rc, _ = _call(native, "perks_stencil2d_noalloc", f, "2d5pt", 2)
     assert rc == -10
     assert "bytes of scratch" in native.last_error()
+
+
+def test_noalloc_allocates_nothing(native, cuda):
+    """After a first call (which may load the kernel's code), further calls,
+    also on a larger field than any before, make no workspace allocation and
+    leave the device's free memory where it was."""
+    import torch
+    L = native.lib()
+    g = torch.Generator(device="cpu").manual_seed(8)
+    small = torch.rand((200, 900), generator=g, dtype=torch.float32).to(cuda)
+    big = torch.rand((1900, 2000), generator=g, dtype=torch.float32).to(cuda)
+    out_big = torch.empty_like(big)
+    rc, _ = _call(native, "perks_stencil2d_noalloc", small, "2ds9pt", 3)
+    assert rc == 0, native.last_error()
+    torch.cuda.synchronize()
+    allocs0 = L.perks_debug_workspace_allocs()
+    free0, _ = torch.cuda.mem_get_info()
+    for steps in (5, 6, 1):
+        rc, _ = _call(native, "perks_stencil2d_noalloc", big, "2ds9pt", steps, out=out_big)
+        assert rc == 0, native.last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert L.perks_debug_workspace_allocs() == allocs0
+    # every buffer of the calls exists before free0 is read, so the device's
+    # free memory only moves if the entry point allocated something
+    assert free1 == free0, (free0, free1)
+    ref, _ = _call(native, "perks_stencil2d", big, "2ds9pt", 1)
+    assert torch.equal(ref.view(torch.uint8), out_big.view(torch.uint8))
