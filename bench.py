@@ -127,6 +127,38 @@ def barrier(ws: int):
         dist.barrier()
 
 
+def extra_cpu():
+    """The CPU port on one thread as well as on all cores (the reference's
+    CPU code is single-threaded), and the FP64 CPU CG per iteration on the
+    2D Laplacian of 2048^2 cells (20 iterations, bounded sample)."""
+    import numpy as np
+    from oracle import oracle as O
+    from perks_gb300 import matrices as M
+    O.build()
+    all_threads = O.num_threads()
+    rng = np.random.default_rng(0)
+    f = rng.random((WY, WX), dtype=np.float32)
+    out = {}
+    prev = O.set_num_threads(1)
+    try:
+        t0 = time.perf_counter()
+        O.stencil(SHAPE, f, 2)
+        dt = time.perf_counter() - t0
+        out["cpu_port_1thread"] = {"value": WY * WX * 2 / dt / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+                                   "sample": f"{SHAPE} fp32 {WY}x{WX}, 2 time steps, oracle C port, 1 thread"}
+        rp, ci, v = M.laplacian_2d(2048)
+        b = np.random.default_rng(1).uniform(-1, 1, len(rp) - 1)
+        for threads in (1, all_threads):
+            O.set_num_threads(threads)
+            t0 = time.perf_counter()
+            O.cg(rp, ci, v, b, max_iter=20, stop=1, tol=0.0, static_iter=True)
+            dt = time.perf_counter() - t0
+            out[f"cpu_cg_lap2d_2048_fp64_{threads}thread_ms_per_iter"] = round(dt * 1e3 / 20, 2)
+    finally:
+        O.set_num_threads(prev)
+    return out
+
+
 def cpu_baseline(seconds_budget: float = 15.0):
     """The oracle (C restatement of the reference's CPU gold code, OpenMP over
     rows) on this host's cores, on a bounded sample of the workload."""
@@ -301,16 +333,23 @@ def main():
         _, st = P.stencil2d(d64, SHAPE, 50, out=o64, kernel="persistent", order="fast")
         extra["persistent_fast_fp64_gcells"] = round(st["gcells_per_s"], 2)
         del d64, o64
+        _, st = P.stencil2d(d_in, SHAPE, 20, out=d_out, kernel="naive")
+        extra["naive_fp32_gcells"] = round(st["gcells_per_s"], 2)
         extra["cached_fraction"] = round(kernel_cached_fraction(P, d_in, d_out), 4)
         extra.update(host_link_gbs(torch, host, hout, d_in, d_out))
+        extra.update(extra_fma_peak(P))
+        extra.update(extra_config1(P, torch, extra.get("fma_peak", {})))
         extra.update(extra_min_domain(P, torch))
         extra.update(extra_3d(P, torch))
         extra.update(extra_cg(P, torch))
+        extra.update(extra_cg_spd_sizes(P, torch))
         extra.update(extra_batch(P, torch))
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline()
+        if not args.no_extra:
+            extra.update(extra_cpu())
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -343,6 +382,50 @@ def host_link_gbs(torch, host, hout, d_in, d_out, reps=5):
         e1.record()
         torch.cuda.synchronize()
         out[tag] = round(src.numel() * src.element_size() * reps / (e0.elapsed_time(e1) * 1e6), 1)
+    return out
+
+
+def extra_fma_peak(P):
+    """Measured FMA throughput (perks_probe_fma_peak): the arithmetic roofline
+    of the FP64 stencils and CG, bound by the FP64 pipe on GB300."""
+    out = {}
+    for dt in ("fp64", "fp32"):
+        best = max((P.fma_peak(dt) for _ in range(3)), key=lambda r: r["fma_per_s"])
+        out[dt] = {"fma_per_s": best["fma_per_s"], "tflops": round(best["tflops"], 3)}
+    return {"fma_peak": out}
+
+
+# FP64 arithmetic operations per cell of 2d5pt in reference order: five
+# products of a weight and a neighbour, four sums, and the exact division by
+# 118 (product with the reciprocal, remainder fma, correction fma); each takes
+# one issue slot of the FP64 pipe, like one FMA.
+FP64_OPS_2D5PT_REF = 12
+
+
+def extra_config1(P, torch, peak, steps=1000):
+    """The plain FP64 configuration: 2d5pt on 1024 x 1024 cells (clamp, the
+    reference driver's check) and 1026 x 1026 with a fixed Dirichlet border,
+    seeded uniform [0,1), 1000 time steps, reference order (bit-identical to
+    the CPU oracle in the tests). Persistent kernel against one launch per
+    step and the naive per-cell kernel; the FP64-pipe fraction counts
+    FP64_OPS_2D5PT_REF operations per cell against the measured FP64 FMA rate.
+    The field (8 MiB) lives in L2, so HBM is not the bound here."""
+    g = torch.Generator(device="cpu").manual_seed(1)
+    f = torch.rand((1026, 1026), generator=g, dtype=torch.float64).cuda()
+    out = {}
+    fma = (peak.get("fp64") or {}).get("fma_per_s")
+    for tag, d, bnd in (("clamp_1024", f[1:-1, 1:-1].contiguous(), "clamp"), ("dirichlet_1026", f, "dirichlet")):
+        o = torch.empty_like(d)
+        row = {}
+        for kernel in ("persistent", "per_step", "naive"):
+            P.stencil2d(d, "2d5pt", 3, out=o, kernel=kernel, boundary=bnd)
+            _, st = P.stencil2d(d, "2d5pt", steps, out=o, kernel=kernel, boundary=bnd)
+            row[f"{kernel}_gcells"] = round(st["gcells_per_s"], 2)
+            if kernel == "persistent":
+                row["persistent_ms"] = round(st["ms"], 3)
+                if fma:
+                    row["fp64_pipe_frac"] = round(st["gcells_per_s"] * 1e9 * FP64_OPS_2D5PT_REF / fma, 4)
+        out[f"config1_2d5pt_fp64_{tag}"] = {"steps": steps, **row}
     return out
 
 
@@ -398,23 +481,62 @@ def extra_cg(P, torch):
         for dt in ("fp64", "mixed"):
             if fmt == "csr":
                 x, res = P.cg_csr(rp, ci, v, b, dtype=dt, tol=1e-10)
+                mb = cg_bytes_csr(len(b), len(ci), dt)
             else:
                 x, res = P.cg_dia(off, data, b, dtype=dt, tol=1e-10)
-            out[f"cg_lap2d_2048_{fmt}_{dt}"] = cg_summary(res)
-    # 3D 7-point Laplacian 160^3 (4.1M rows) and a random SPD CSR matrix
-    # (n = 1e6, power-law rows of 3..60 entries, diagonally dominant), CSR input
-    for tag, (rp, ci, v) in (("lap3d_160", M.laplacian_3d(160)), ("spd_1e6", M.random_spd(1_000_000, 7))):
-        b = np.random.default_rng(1).uniform(-1, 1, len(rp) - 1)
-        for dt in ("fp64", "mixed"):
-            x, res = P.cg_csr(rp, ci, v, b, dtype=dt, tol=1e-10)
-            out[f"cg_{tag}_csr_{dt}"] = cg_summary(res)
+                mb = cg_bytes_dia(len(b), len(off), dt)
+            out[f"cg_lap2d_2048_{fmt}_{dt}"] = cg_summary(res, mb)
+    # 3D 7-point Laplacian 160^3 (4.1M rows), CSR input
+    rp, ci, v = M.laplacian_3d(160)
+    b = np.random.default_rng(1).uniform(-1, 1, len(rp) - 1)
+    for dt in ("fp64", "mixed"):
+        x, res = P.cg_csr(rp, ci, v, b, dtype=dt, tol=1e-10)
+        out[f"cg_lap3d_160_csr_{dt}"] = cg_summary(res, cg_bytes_csr(len(b), len(ci), dt))
     return out
 
 
-def cg_summary(res):
-    return {"ms": round(res["ms"], 2), "iterations": res["iterations"],
-            "us_per_iter": round(1e3 * res["ms"] / max(1, res["iterations"]), 2),
-            "true_rel_res": res["true_rel_res"]}
+def extra_cg_spd_sizes(P, torch):
+    """CG on the random sparse SPD matrices (power-law rows of 3..60 entries,
+    mean about 14, N(0,1) off-diagonals, diagonally dominant), n = 1e5 to 2e6,
+    CSR input, FP64 against mixed precision at the same 1e-10 relative
+    residual."""
+    import numpy as np
+    from perks_gb300 import matrices as M
+    out = {}
+    for n, tag in ((100_000, "1e5"), (300_000, "3e5"), (1_000_000, "1e6"), (2_000_000, "2e6")):
+        rp, ci, v = M.random_spd(n, 7)
+        b = np.random.default_rng(1).uniform(-1, 1, n)
+        for dt in ("fp64", "mixed"):
+            P.cg_csr(rp, ci, v, b, dtype=dt, tol=1e-10)  # first call: setup of this size
+            x, res = P.cg_csr(rp, ci, v, b, dtype=dt, tol=1e-10)
+            out[f"cg_spd_{tag}_csr_{dt}"] = cg_summary(res, cg_bytes_csr(n, len(ci), dt))
+    return out
+
+
+def cg_bytes_csr(n, nnz, dtype):
+    """Algorithmic bytes of one CG iteration, the reference's formula
+    (conjugateGradient/cg_driver.cu:360-361): nnz (value + int32 column) +
+    (n+1) row pointers + six vector passes, at the iteration's working
+    precision (FP32 for the inner iterations of mixed precision)."""
+    sv = 8 if dtype == "fp64" else 4
+    return nnz * (sv + 4) + 4 * (n + 1) + 6 * n * sv
+
+
+def cg_bytes_dia(n, ndiag, dtype):
+    sv = 8 if dtype == "fp64" else 4
+    return ndiag * n * sv + 6 * n * sv
+
+
+def cg_summary(res, bytes_per_iter=None):
+    it = max(1, res["iterations"])
+    out = {"ms": round(res["ms"], 2), "iterations": res["iterations"],
+           "us_per_iter": round(1e3 * res["ms"] / it, 2), "true_rel_res": res["true_rel_res"]}
+    if bytes_per_iter:
+        peak, src = measured_hbm_peak()
+        gbs = bytes_per_iter * it / (res["ms"] * 1e-3) / 1e9
+        out["roofline"] = {"bound": "hbm", "bytes_per_iter": bytes_per_iter, "achieved": round(gbs, 1),
+                           "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4), "peak_source": src}
+    return out
 
 
 def extra_batch(P, torch, n_jobs=512, steps=100, seed=42):

@@ -73,7 +73,10 @@ typedef enum {
 
 typedef enum {
   PERKS_KERNEL_PERSISTENT = 0, /* one cooperative launch for all steps, rows/planes kept on chip */
-  PERKS_KERNEL_PER_STEP = 1    /* one launch per time step, nothing kept on chip (comparator) */
+  PERKS_KERNEL_PER_STEP = 1,   /* one launch per time step, nothing kept on chip (comparator) */
+  PERKS_KERNEL_NAIVE = 2       /* 2D only: one launch per step, one thread per cell reading every
+                                  neighbour from global memory (comparator: the reference's
+                                  kernel2d_restrict, stencil/2dstencil/jacobi-naive.cu:7-106) */
 } perks_kernel;
 
 /* --------------------------------------------------------------- stencils */
@@ -335,6 +338,15 @@ PERKS_API void perks_batch_plan_destroy(perks_batch_plan plan);
 PERKS_API int perks_mtx_size(const char* path, int* rows, int* cols, long long* nnz);
 PERKS_API int perks_mtx_read_csr(const char* path, int rows, long long nnz_cap, int* row_ptr, int* col,
                                  double* val, long long* nnz);
+
+/* ------------------------------------------------------------ measurement */
+/* FMA throughput of this GPU in the given precision (PERKS_FP64 or
+ * PERKS_FP32), in fused multiply-adds per second (a FLOP rate is twice it):
+ * eight independent FMA chains per thread, four 256-thread CTAs per SM, one
+ * launch of about 0.1 s. The arithmetic roofline of the FP64 stencils and
+ * CG, which are bound by the FP64 pipe on GB300 rather than by HBM. `ms`
+ * (may be NULL) receives the timed launch's duration. */
+PERKS_API int perks_probe_fma_peak(int dtype, double* fma_per_s, double* ms);
 
 /* ------------------------------------------------------------------ misc */
 PERKS_API const char* perks_last_error(void);     /* thread-local message of the last failure */

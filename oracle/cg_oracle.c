@@ -145,6 +145,9 @@ static int cg64(int n, spmv64_fn A, const void* ctx, const double* b, double* x,
   int status = 0;
   memcpy(r, b, sizeof(double) * n);
   A(ctx, x, Ax);
+  /* element-wise loops run in parallel (each element's arithmetic is the
+   * same whatever the thread); the dot products stay sequential */
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < n; i++) r[i] = -1.0 * Ax[i] + r[i];
   double r1 = dot_f64(r, r, n), r0 = 0.0;
   int k = 1;
@@ -156,6 +159,7 @@ static int cg64(int n, spmv64_fn A, const void* ctx, const double* b, double* x,
     }
     if (k > 1) {
       double beta = r1 / r0;
+#pragma omp parallel for schedule(static)
       for (int i = 0; i < n; i++) p[i] = r[i] + beta * p[i];
     } else {
       memcpy(p, r, sizeof(double) * n);
@@ -164,8 +168,11 @@ static int cg64(int n, spmv64_fn A, const void* ctx, const double* b, double* x,
     double dot = dot_f64(p, Ax, n);
     if (!(dot > 0.0) || !isfinite(dot)) { status = -1; break; }
     double a = r1 / dot;
-    for (int i = 0; i < n; i++) x[i] = a * p[i] + x[i];
-    for (int i = 0; i < n; i++) r[i] = -a * Ax[i] + r[i];
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++) {
+      x[i] = a * p[i] + x[i];
+      r[i] = -a * Ax[i] + r[i];
+    }
     r0 = r1;
     r1 = dot_f64(r, r, n);
     if (trace) trace[k] = r1;

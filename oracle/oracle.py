@@ -114,6 +114,15 @@ def num_threads() -> int:
     return lib().oracle_num_threads()
 
 
+def set_num_threads(n: int) -> int:
+    """Threads of the oracle's parallel loops from now on (n <= 0: all
+    cores); returns the previous count."""
+    L = lib()
+    L.oracle_set_num_threads.restype = _I
+    L.oracle_set_num_threads.argtypes = [_I]
+    return L.oracle_set_num_threads(int(n))
+
+
 def ref_available(shape: str | None = None) -> bool:
     name = "libref_cg.so" if shape is None else f"libref_{shape}.so"
     return os.path.exists(os.path.join(REF_DIR, name))

@@ -328,3 +328,18 @@ int oracle_num_threads(void) {
   return 1;
 #endif
 }
+
+/* Threads of the parallel loops from now on (n <= 0: all cores); returns the
+ * previous count. For timing the port on one core as well as on all. */
+int oracle_set_num_threads(int n) {
+#ifdef _OPENMP
+  static int all = 0;
+  if (!all) all = omp_get_num_procs();
+  const int prev = omp_get_max_threads();
+  omp_set_num_threads(n > 0 ? n : all);
+  return prev;
+#else
+  (void)n;
+  return 1;
+#endif
+}

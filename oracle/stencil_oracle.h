@@ -12,6 +12,7 @@ int oracle_stencil2d_f64(int shape, const double* in, int wy, int wx, double* ou
 int oracle_stencil3d_f32(int shape, const float* in, int h, int wy, int wx, float* out, int steps, int boundary);
 int oracle_stencil3d_f64(int shape, const double* in, int h, int wy, int wx, double* out, int steps, int boundary);
 int oracle_num_threads(void);
+int oracle_set_num_threads(int n);
 
 void oracle_spmv_csr_f64(int n, const int* rp, const int* ci, const double* v, const double* x, double* y);
 void oracle_spmv_csr_f32(int n, const int* rp, const int* ci, const float* v, const float* x, float* y);

@@ -23,3 +23,14 @@ def launch_count() -> int:
 
 def reset_launch_count() -> None:
     _native.lib().perks_reset_launch_count()
+
+
+def fma_peak(dtype: str = "fp64") -> dict:
+    """Measured FMA throughput of the current GPU in 'fp64' or 'fp32'
+    (perks_probe_fma_peak): fused multiply-adds per second, the FLOP rate
+    (twice that) in TFLOP/s, and the timed launch's milliseconds."""
+    import ctypes
+    rate, ms = ctypes.c_double(), ctypes.c_double()
+    _native.check(_native.lib().perks_probe_fma_peak(_native.FP64 if dtype == "fp64" else _native.FP32,
+                                                     ctypes.byref(rate), ctypes.byref(ms)))
+    return {"dtype": dtype, "fma_per_s": rate.value, "tflops": 2e-12 * rate.value, "ms": ms.value}

@@ -29,7 +29,7 @@ HALO = {"2d5pt": 1, "2ds9pt": 2, "2d13pt": 3, "2d17pt": 4, "2d21pt": 5, "2ds25pt
 FP32, FP64, MIXED = 0, 1, 2
 CLAMP, DIRICHLET = 0, 1
 ORDER_REFERENCE, ORDER_FAST = 0, 1
-KERNEL_PERSISTENT, KERNEL_PER_STEP = 0, 1
+KERNEL_PERSISTENT, KERNEL_PER_STEP, KERNEL_NAIVE = 0, 1, 2
 STOP_ABS_RR, STOP_REL = 0, 1
 
 
@@ -116,6 +116,7 @@ SIGNATURES = {
                                ctypes.POINTER(ctypes.c_longlong)]),
     "perks_mtx_read_csr": (c_int, [ctypes.c_char_p, c_int, ctypes.c_longlong, c_void_p, c_void_p, c_void_p,
                                    ctypes.POINTER(ctypes.c_longlong)]),
+    "perks_probe_fma_peak": (c_int, [c_int, ctypes.POINTER(c_double), ctypes.POINTER(c_double)]),
     "perks_last_error": (ctypes.c_char_p, []),
     "perks_status_string": (ctypes.c_char_p, [c_int]),
     "perks_abi_version": (c_int, []),

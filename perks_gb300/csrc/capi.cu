@@ -35,7 +35,8 @@ static int check_opts(const perks_stencil_opts* o, bool want3d) {
     return fail(PERKS_ERR_INVALID_ARG, "unknown boundary mode");
   if (o->order != PERKS_ORDER_REFERENCE && o->order != PERKS_ORDER_FAST)
     return fail(PERKS_ERR_INVALID_ARG, "unknown evaluation order");
-  if (o->kernel != PERKS_KERNEL_PERSISTENT && o->kernel != PERKS_KERNEL_PER_STEP)
+  if (o->kernel != PERKS_KERNEL_PERSISTENT && o->kernel != PERKS_KERNEL_PER_STEP &&
+      !(o->kernel == PERKS_KERNEL_NAIVE && !want3d))
     return fail(PERKS_ERR_INVALID_ARG, "unknown kernel kind");
   return PERKS_OK;
 }

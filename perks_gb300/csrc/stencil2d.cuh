@@ -462,4 +462,24 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
   }
 }
 
+// Naive comparator (the reference's kernel2d_restrict,
+// stencil/2dstencil/jacobi-naive.cu:7-106): one thread per cell, every
+// neighbour read from global memory at its clamped index, one launch per
+// time step, nothing staged on chip. Same arithmetic as the other kernels.
+template <class T, int SHAPE, bool FAST, int FIN>
+__global__ void __launch_bounds__(256) stencil2d_naive(const T* __restrict__ fin, T* __restrict__ fout, int wy,
+                                                       int wx, int pitch, int dirichlet) {
+  constexpr int H = ShapeInfo<SHAPE>::H;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= wx || y >= wy) return;
+  auto u = [&](int, int dy, int dx) -> T {
+    const int yy = min(max(y + dy, 0), wy - 1), xx = min(max(x + dx, 0), wx - 1);
+    return fin[size_t(yy) * pitch + xx];
+  };
+  T o = stencil_point<T, SHAPE, FAST, FIN>(u);
+  if (dirichlet && (y < H || y >= wy - H || x < H || x >= wx - H)) o = fin[size_t(y) * pitch + x];
+  fout[size_t(y) * pitch + x] = o;
+}
+
 }  // namespace perks

@@ -53,6 +53,7 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   if (!dev) return PERKS_ERR_NO_DEVICE;
   cudaStream_t s = static_cast<cudaStream_t>(o.stream);
   const bool persistent = o.kernel == PERKS_KERNEL_PERSISTENT;
+  const bool naive = o.kernel == PERKS_KERNEL_NAIVE;
   const int ctas = o.ctas > 0 ? std::min(o.ctas, dev->sms) : dev->sms;
   const long long warps = (long long)ctas * Cf::NW;
   const int ns = ceil_div(wx, Cf::SW);
@@ -121,7 +122,19 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   PERKS_CUDA(cudaEventCreate(&e1));
   PERKS_CUDA(cudaEventRecord(e0, s));
   int launches = 0;
-  if (persistent) {
+  if (naive) {
+    const dim3 blk(32, 8), grd(unsigned(ceil_div(wx, 32)), unsigned(ceil_div(wy, 8)));
+    for (int t = 0; t < steps; t++)
+      stencil2d_naive<T, SHAPE, FAST, Cf::FIN><<<grd, blk, 0, s>>>((t & 1) ? f1 : f0, (t & 1) ? f0 : f1, wy, wx,
+                                                                   pitch, p.dirichlet);
+    launches = steps;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return cuda_fail(e, "stencil2d naive launch");
+    }
+  } else if (persistent) {
     int nb = 0;
     PERKS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, Cf::NT, smem));
     if (nb * dev->sms < grid) {

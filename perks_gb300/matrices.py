@@ -99,13 +99,13 @@ def random_spd(n: int, seed: int = 0, lo: int = 3, hi: int = 60, mean_degree: fl
     r = np.concatenate([a, b])
     c = np.concatenate([b, a])
     v = np.concatenate([w, w])
-    diag = np.zeros(n)
-    np.add.at(diag, r, np.abs(v))
+    # bincount adds the weights in array order, as np.add.at would
+    diag = np.bincount(r, weights=np.abs(v), minlength=n)
     diag += rng.uniform(0.1, 1.0, n)
     r = np.concatenate([r, np.arange(n)])
     c = np.concatenate([c, np.arange(n)])
     v = np.concatenate([v, diag])
-    order = np.lexsort((c, r))
+    order = np.argsort(r * n + c)  # (row, column) keys are unique: the row-major order
     r, c, v = r[order], c[order], v[order]
     row_ptr = np.zeros(n + 1, np.int64)
     np.cumsum(np.bincount(r, minlength=n), out=row_ptr[1:])

@@ -4,6 +4,7 @@
   python -m perks_gb300.profile cg --matrix lap2d --n 512 --dtype fp64 --iters 20
   python -m perks_gb300.profile batch --jobs 512 --steps 100
   python -m perks_gb300.profile sweep --steps 1000     # every stencil shape, one JSON line each
+  python -m perks_gb300.profile fmapeak                # FP64 and FP32 FMA throughput of this GPU
 
 Runs one warm-up call, then exactly one call of the requested size, and
 prints its stats as one JSON line. The warm-up uses the same kernel with 2
@@ -64,7 +65,7 @@ def _sweep(a):
         for dtn, dt in (("f32", torch.float32), ("f64", torch.float64)):
             d = f64.to(dt).cuda()
             o = torch.empty_like(d)
-            for kernel in ("persistent", "per_step"):
+            for kernel in ("persistent", "per_step") + (("naive",) if len(dims) == 2 else ()):
                 fn(d, shape, 2, out=o, kernel=kernel)
                 torch.cuda.synchronize()
                 _, st = fn(d, shape, a.steps, out=o, kernel=kernel)
@@ -103,6 +104,18 @@ def _cg(a):
     return {"matrix": a.matrix, "n": a.n, "format": a.format, "dtype": a.dtype, **res}
 
 
+def _fmapeak(a):
+    """FP64 and FP32 FMA throughput (perks_probe_fma_peak), best of a.reps."""
+    from . import fma_peak
+    out = {}
+    for dt in ("fp64", "fp32"):
+        runs = [fma_peak(dt) for _ in range(a.reps)]
+        best = max(runs, key=lambda r: r["fma_per_s"])
+        out[dt] = {"fma_per_s": best["fma_per_s"], "tflops": round(best["tflops"], 3),
+                   "ms": round(best["ms"], 3), "runs": [round(r["tflops"], 3) for r in runs]}
+    return out
+
+
 def _batch(a):
     import torch
     from .batch import BatchPlan, synthetic_workload
@@ -122,7 +135,7 @@ def main(argv=None):
     s.add_argument("--dims", required=True, help="wy,wx or h,wy,wx")
     s.add_argument("--dtype", default="f32", choices=["f32", "f64"])
     s.add_argument("--order", default="reference", choices=["reference", "fast"])
-    s.add_argument("--kernel", default="persistent", choices=["persistent", "per_step"])
+    s.add_argument("--kernel", default="persistent", choices=["persistent", "per_step", "naive"])
     s.add_argument("--l2-sweep", action="store_true")
     s.add_argument("--steps", type=int, default=3)
     c = sub.add_parser("cg")
@@ -141,8 +154,10 @@ def main(argv=None):
     bt.add_argument("--seed", type=int, default=42)
     bt.add_argument("--threads", type=int, default=1024, help="threads per CTA (0 = autotune)")
     bt.add_argument("--ctas", type=int, default=1, help="CTAs per SM (0 = autotune)")
+    fp = sub.add_parser("fmapeak")
+    fp.add_argument("--reps", type=int, default=5)
     a = ap.parse_args(argv)
-    out = {"stencil": _stencil, "cg": _cg, "batch": _batch, "sweep": _sweep}[a.what](a)
+    out = {"stencil": _stencil, "cg": _cg, "batch": _batch, "sweep": _sweep, "fmapeak": _fmapeak}[a.what](a)
     print(json.dumps(out, default=str), flush=True)
 
 

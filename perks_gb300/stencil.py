@@ -27,7 +27,7 @@ def _opts(shape: str, dtype, order="reference", kernel="persistent", boundary="c
     dt = N.FP64 if np.dtype(dtype) == np.float64 else N.FP32
     N.lib().perks_stencil_default_opts(ctypes.byref(o), N.SHAPES[shape], dt)
     o.order = {"reference": N.ORDER_REFERENCE, "fast": N.ORDER_FAST}[order]
-    o.kernel = {"persistent": N.KERNEL_PERSISTENT, "per_step": N.KERNEL_PER_STEP}[kernel]
+    o.kernel = {"persistent": N.KERNEL_PERSISTENT, "per_step": N.KERNEL_PER_STEP, "naive": N.KERNEL_NAIVE}[kernel]
     o.boundary = {"clamp": N.CLAMP, "dirichlet": N.DIRICHLET}[boundary]
     o.cache_rows = int(cache_rows)
     o.l2_sweep = int(bool(l2_sweep))

@@ -69,6 +69,31 @@ def test_cg_resume_after_cap(native, cuda, dtype, kernel):
     assert r3["iterations"] == K and bits_equal(x3.cpu().numpy(), x_full.cpu().numpy())
 
 
+@pytest.mark.parametrize("kernel", ["persistent", "per_step"])
+@pytest.mark.parametrize("fmt", ["csr", "dia"])
+def test_cg_resume_matches_oracle(native, cuda, oracle, kernel, fmt):
+    """A solve stopped by its iteration cap halfway and resumed from the
+    checkpoint ends where the FP64 oracle's uninterrupted solve ends: the same
+    iteration count (within 1), a true relative residual below the tolerance
+    recomputed on the host with the oracle's SpMV, and the oracle's solution
+    (this shifted Laplacian is well conditioned, so solutions that meet the
+    tolerance agree closely)."""
+    prob = _problem(fmt)
+    (rp, ci, v), b, _ = prob
+    xo, it, _, _ = oracle.cg(rp, ci, v, b, max_iter=5000, stop=1, tol=1e-10)
+    ck = native.CgCheckpoint()
+    x1, r1 = _solve(native, cuda, prob, "fp64", tol=1e-10, kernel=kernel, max_iter=it // 2, check=False,
+                    checkpoint=ck)
+    assert r1["status"] == -18 and ck.k == it // 2
+    ck2 = native.CgCheckpoint.from_host(ck.to_host(), device=cuda)
+    x2, r2 = _solve(native, cuda, prob, "fp64", x0=x1.cpu().numpy(), tol=1e-10, kernel=kernel, checkpoint=ck2)
+    assert abs(r2["iterations"] - it) <= 1, (r2, it)
+    x = x2.cpu().numpy()
+    r = b - oracle.spmv_csr(rp, ci, v, x)
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 1e-10 * 1.05
+    assert np.allclose(x, xo, rtol=1e-8, atol=1e-10)
+
+
 def test_cg_checkpoint_rejects_misuse(native, cuda):
     prob = _problem("csr")
     ck = native.CgCheckpoint()

@@ -70,7 +70,7 @@ def test_2d_ragged_vs_oracle(native, cuda, oracle, shape, dt):
         ref = oracle.stencil(shape, f, steps)
         for kw in ({"kernel": "persistent", "ctas": ctas}, {"kernel": "per_step", "ctas": ctas},
                    {"kernel": "persistent", "ctas": ctas, "l2_sweep": True},
-                   {"kernel": "persistent", "ctas": ctas, "cache_rows": 0}):
+                   {"kernel": "persistent", "ctas": ctas, "cache_rows": 0}, {"kernel": "naive"}):
             g, st = run(native, cuda, f, shape, steps, **kw)
             assert bits_equal(g, ref), (shape, dims, kw, steps, np.nanmax(np.abs(g - ref)))
 
@@ -115,8 +115,10 @@ def test_3d_work_split(native, cuda, oracle, dt, shape):
 
 
 @pytest.mark.parametrize("shape", ["2d5pt", "2ds25pt", "2d25pt", "3d7pt", "3d27pt", "poisson"])
-@pytest.mark.parametrize("kernel", ["persistent", "per_step"])
+@pytest.mark.parametrize("kernel", ["persistent", "per_step", "naive"])
 def test_dirichlet_vs_oracle(native, cuda, oracle, shape, kernel):
+    if kernel == "naive" and not shape.startswith("2d"):
+        pytest.skip("the naive comparator is 2D only, as in the reference")
     dims = (300, 517) if shape.startswith("2d") else (20, 37, 70)
     f = np.random.default_rng(5).random(dims)
     g, _ = run(native, cuda, f, shape, 5, kernel=kernel, boundary="dirichlet")
