@@ -230,6 +230,8 @@ typedef struct {
   double true_rel_res;   /* ||b - A x|| / ||b|| recomputed in FP64 on the device after the solve */
   double ms;             /* device time of the solve */
   int launches;
+  int layout;            /* matrix layout the iteration ran on: 0 CSR as given (lane groups per row),
+                            1 DIA, 2 ELL, 3 SELL (copies made at the start of the solve) */
 } perks_cg_result;
 
 PERKS_API void perks_cg_default_opts(perks_cg_opts* opts);

@@ -58,7 +58,7 @@ class CgOpts(ctypes.Structure):
 
 class CgResult(ctypes.Structure):
     _fields_ = [("iterations", c_int), ("outer", c_int), ("rr", c_double), ("true_rel_res", c_double),
-                ("ms", c_double), ("launches", c_int)]
+                ("ms", c_double), ("launches", c_int), ("layout", c_int)]
 
 
 class Job(ctypes.Structure):

@@ -51,16 +51,30 @@ namespace perks {
 constexpr int kCgThreads = 1024;
 constexpr int kMaxDiag = 32;
 
+// SELL-C-sigma (Kreutzer et al., "A unified sparse matrix data format for
+// efficient general sparse matrix-vector multiplication on modern processors
+// with wide SIMD units", SIAM J. Sci. Comput. 36(5), 2014) with C = 32: rows
+// sorted by length (longest first) within windows of kSellWindow rows, cut
+// into slices of 32 rows; a slice stores its entries column-major, entry k of
+// slot l at sl_ptr[slice] + 32 k + l, padded to its longest row with column =
+// the slot's own row and value 0. One lane computes one row in CSR entry
+// order, so a warp's loads of values and columns are coalesced and rows of
+// similar length share a warp.
+constexpr int kSellWindow = 1024;
+
 struct CgMat {
-  int n, nnz, fmt;        // fmt 0 = CSR, 1 = DIA, 2 = ELL (column-major, ew entries per row)
+  int n, nnz, fmt;        // fmt 0 = CSR, 1 = DIA, 2 = ELL (column-major, ew entries per row), 3 = SELL
   const int* rp;          // CSR
   const int* ci;
   const void* val;        // CSR values or DIA data (dtype of the solve, FP64 for mixed)
   int ndiag;
   int off[kMaxDiag];
-  const int* eci;         // ELL column indices [ew][n]
+  const int* eci;         // ELL column indices [ew][n]; SELL column indices
   int ew;
   int grp;                // CSR: lanes per row in the SpMV phase (4, 8, 16 or 32)
+  const int* sl_ptr;      // SELL: [nslices + 1] first entry of each slice
+  const int* sl_row;      // SELL: [nslices * 32] row of each slot (n: an empty padding slot)
+  int nslices;
 };
 
 struct CgParams {
@@ -101,6 +115,37 @@ __device__ __forceinline__ int cg_split(const CgMat& A, int c, int ncta) {
     else hi = mid;
   }
   return lo;
+}
+
+// SELL: first slice of CTA `c`, splitting slices + their padded entries evenly.
+__device__ __forceinline__ int sell_split(const CgMat& A, int c, int ncta) {
+  const long long total = (long long)A.sl_ptr[A.nslices] + 32ll * A.nslices;
+  const long long target = total * c / ncta;
+  int lo = 0, hi = A.nslices;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if ((long long)A.sl_ptr[mid] + 32ll * mid < target) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// SELL SpMV over slices [s0, s1): warp w of the CTA takes slices s0 + w,
+// s0 + w + nwarps, ...; lane l computes the row of slot l in CSR entry order
+// (padding entries add fma(0, x_row, acc) = acc: the sum is never -0) and
+// runs epi(row, sum) for a slot that holds a row.
+template <class XV, class MV, class XF, class Epi>
+__device__ __forceinline__ void sell_rows(const CgMat& A, const MV* __restrict__ val, int s0, int s1, const XF& xv,
+                                          Epi&& epi) {
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int s = s0 + (threadIdx.x >> 5); s < s1; s += nw) {
+    const int e0 = __ldg(A.sl_ptr + s), e1 = __ldg(A.sl_ptr + s + 1);
+    const int row = __ldg(A.sl_row + s * 32 + lane);
+    XV acc = XV(0);
+#pragma unroll 4
+    for (int e = e0 + lane; e < e1; e += 32) acc = fma(XV(__ldg(val + e)), xv(__ldg(A.eci + e)), acc);
+    if (row < A.n) epi(row, acc);
+  }
 }
 
 // Row i of A times a vector given by xv(column). Accumulates in the working
@@ -339,14 +384,24 @@ __device__ __forceinline__ void csr_rows_grouped(const CgMat& A, const MV* __res
 }
 
 // SpMV phase rows: DIA and ELL in groups of four rows per thread (f4; the
-// ragged ends row by row), CSR by lane groups. e1(i, row sum) finishes a row.
+// ragged ends row by row), CSR by lane groups, SELL by slices (the CTA's
+// slice range sr; rows in slot order). e1(i, row sum) finishes a row.
 template <int FMT, class XV, class MV, class XF, class F4, class E1>
 __device__ __forceinline__ void cg_rows_spmv(const CgMat& A, const MV* __restrict__ val, const XF& xv, int row0,
-                                             int row1, F4&& f4, E1&& e1) {
-  if ((FMT >= 0 ? FMT : A.fmt) != 0)
-    cg_rows4(row0, row1, true, f4, [&](int i) { e1(i, spmv_row_f<XV, FMT>(A, val, xv, i)); });
-  else
+                                             int row1, int2 sr, F4&& f4, E1&& e1) {
+  static_assert(FMT >= 0, "format fixed at compile time");
+  if constexpr (FMT == 3)
+    sell_rows<XV>(A, val, sr.x, sr.y, xv, e1);
+  else if constexpr (FMT == 0)
     csr_rows_grouped<XV>(A, val, row0, row1, xv, e1);
+  else
+    cg_rows4(row0, row1, true, f4, [&](int i) { e1(i, spmv_row_f<XV, FMT>(A, val, xv, i)); });
+}
+// The CTA's SELL slice range (unused for other formats).
+template <int FMT>
+__device__ __forceinline__ int2 cta_slices(const CgMat& A) {
+  if constexpr (FMT == 3) return make_int2(sell_split(A, blockIdx.x, gridDim.x), sell_split(A, blockIdx.x + 1, gridDim.x));
+  else return make_int2(0, 0);
 }
 __device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
   const float4 t = *reinterpret_cast<const float4*>(p);
@@ -425,7 +480,7 @@ template <class T, int FMT>
 __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_constant__ CgParams P) {
   // FP32 forms p where the SpMV gathers it, except for CSR: there the random
   // gathers dominate, and gathering p_old and r instead of p doubles them
-  constexpr bool FUSE = sizeof(T) == 4 && FMT != 0;
+  constexpr bool FUSE = sizeof(T) == 4 && FMT != 0 && FMT != 3;
   const CgMat& A = P.A;
   const T* __restrict__ val = static_cast<const T*>(A.val);
   const T* __restrict__ b = static_cast<const T*>(P.b);
@@ -434,6 +489,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
   T* __restrict__ Ap = static_cast<T*>(P.Ap);
   const int G = gridDim.x;
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
+  const int2 sr = cta_slices<FMT>(A);
   GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G), P.ctl}};
   const int tid = threadIdx.x, nt = blockDim.x;
   const bool xvec = aligned16(x);  // the caller's solution vector
@@ -450,14 +506,18 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
   } else {
     // r = b - A x ; rr = r.r ; bb = b.b  (per-thread sums in T, then double)
     T rr_t = T(0), bb_t = T(0);
-    CG_ROWS(i, {
-      const T ax = spmv_row<FMT>(A, val, x, i);
+    auto init_row = [&](int i, T ax) {
       const T bi = b[i];
       const T ri = T(-1) * ax + bi;
       r[i] = ri;
       rr_t = fma(ri, ri, rr_t);
       bb_t = fma(bi, bi, bb_t);
-    })
+    };
+    if constexpr (FMT == 3) {
+      sell_rows<T>(A, val, sr.x, sr.y, [x](int c) { return x[c]; }, init_row);
+    } else {
+      CG_ROWS(i, { init_row(i, spmv_row<FMT>(A, val, x, i)); })
+    }
     double rr = double(rr_t);
     bb = double(bb_t);
     if (!gs.sum2(0, rr, bb)) return;
@@ -481,7 +541,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
         const T beta = r1 / r0;
         const T* __restrict__ po = static_cast<const T*>(P.p[(k + 1) & 1]);
         auto pg = [&](int c) { return fma(beta, po[c], r[c]); };
-        cg_rows_spmv<FMT, T>(A, val, pg, row0, row1, [&](int i) {
+        cg_rows_spmv<FMT, T>(A, val, pg, row0, row1, sr, [&](int i) {
           T av[4], pov[4], rv[4], pv[4];
           spmv4<T, FMT>(A, val, v4, pg, i, av);
           ld4(po + i, pov);
@@ -501,7 +561,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
         });
       } else {
         auto rg = [&](int c) { return r[c]; };
-        cg_rows_spmv<FMT, T>(A, val, rg, row0, row1, [&](int i) {
+        cg_rows_spmv<FMT, T>(A, val, rg, row0, row1, sr, [&](int i) {
           T av[4], rv[4];
           spmv4<T, FMT>(A, val, v4, rg, i, av);
           ld4(r + i, rv);
@@ -536,7 +596,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
       }
       if (!gs.gb.sync()) return;
       auto pg = [&](int c) { return p[c]; };
-      cg_rows_spmv<FMT, T>(A, val, pg, row0, row1, [&](int i) {
+      cg_rows_spmv<FMT, T>(A, val, pg, row0, row1, sr, [&](int i) {
         T av[4], pv[4];
         spmv4<T, FMT>(A, val, v4, pg, i, av);
         ld4(p + i, pv);
@@ -618,6 +678,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
   float* __restrict__ xs = P.xs;
   const int G = gridDim.x;
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
+  const int2 sr = cta_slices<FMT>(A);
   GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G), P.ctl}};
   const int tid = threadIdx.x, nt = blockDim.x;
   const bool v4 = A.fmt != 0 && (A.n & 3) == 0 && aligned16(A.eci);  // val32 (workspace) is aligned
@@ -653,9 +714,9 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
     // values its owner stores are the same fma)
     float* __restrict__ p = static_cast<float*>(P.p[k & 1]);
     float pap_t = 0.0f;
-    if constexpr (FMT == 0) {
-      // CSR: p in its own pass (same values as the fused form), so that the
-      // SpMV gathers one vector instead of two
+    if constexpr (FMT == 0 || FMT == 3) {
+      // CSR / SELL: p in its own pass (same values as the fused form), so
+      // that the SpMV gathers one vector instead of two
       const float beta = k > 1 ? float(rr / rr0) : 0.0f;
       const float* __restrict__ po = static_cast<const float*>(P.p[(k + 1) & 1]);
       cg_rows4(row0, row1, true, [&](int i) {
@@ -673,7 +734,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       }, [&](int i) { p[i] = k > 1 ? fmaf(beta, po[i], r[i]) : r[i]; });
       if (!gs.gb.sync()) return;
       auto pgat = [&](int c) { return p[c]; };
-      cg_rows_spmv<FMT, float>(A, val32, pgat, row0, row1, [&](int) {}, [&](int i, float api) {
+      cg_rows_spmv<FMT, float>(A, val32, pgat, row0, row1, sr, [&](int) {}, [&](int i, float api) {
         Ap[i] = api;
         pap_t = fmaf(p[i], api, pap_t);
       });
@@ -681,7 +742,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       const float beta = float(rr / rr0);
       const float* __restrict__ po = static_cast<const float*>(P.p[(k + 1) & 1]);
       auto pg = [&](int c) { return fmaf(beta, po[c], r[c]); };
-      cg_rows_spmv<FMT, float>(A, val32, pg, row0, row1, [&](int i) {
+      cg_rows_spmv<FMT, float>(A, val32, pg, row0, row1, sr, [&](int i) {
         float av[4], pov[4], rv[4], pv[4];
         spmv4<float, FMT>(A, val32, v4, pg, i, av);
         ld4(po + i, pov);
@@ -701,7 +762,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       });
     } else {
       auto rg = [&](int c) { return r[c]; };
-      cg_rows_spmv<FMT, float>(A, val32, rg, row0, row1, [&](int i) {
+      cg_rows_spmv<FMT, float>(A, val32, rg, row0, row1, sr, [&](int i) {
         float av[4], rv[4];
         spmv4<float, FMT>(A, val32, v4, rg, i, av);
         ld4(r + i, rv);
@@ -1000,6 +1061,80 @@ __global__ void dia_build(CgMat D, const int* rp, const int* ci, const SV* val, 
     }
   }
 }
+// SELL setup (kSellWindow threads per window of rows): sort the window's rows
+// by length, longest first, ties by row (a bitonic sort of 64-bit keys in
+// shared memory); write each slot's row (n for the slots after the last row)
+// and each slice's width, the length of its first, longest row.
+__global__ void __launch_bounds__(kSellWindow) sell_sort(const int* rp, int n, int* sl_row, int* width) {
+  __shared__ unsigned long long key[kSellWindow];
+  const int t = threadIdx.x, base = blockIdx.x * kSellWindow;
+  const int len = base + t < n ? rp[base + t + 1] - rp[base + t] : -1;
+  const unsigned inv = len < 0 ? 0xffffffffu : 0x7fffffffu - unsigned(len);  // ascending = longest first
+  key[t] = (static_cast<unsigned long long>(inv) << 32) | unsigned(t);
+  __syncthreads();
+  for (int k = 2; k <= kSellWindow; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const int o = t ^ j;
+      if (o > t) {
+        const unsigned long long a = key[t], b = key[o];
+        if ((a > b) == ((t & k) == 0)) {
+          key[t] = b;
+          key[o] = a;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  const int row = base + int(key[t] & 0xffffffffu);
+  const bool real = row < n;
+  sl_row[base + t] = real ? row : n;
+  if ((t & 31) == 0) width[blockIdx.x * (kSellWindow / 32) + (t >> 5)] = real ? rp[row + 1] - rp[row] : 0;
+}
+// sl_ptr[s] = 32 * (width[0] + ... + width[s-1]) for s <= ns; *total = the
+// sum in 64 bits (the caller rejects layouts past int32). One CTA.
+__global__ void __launch_bounds__(1024) sell_scan(const int* width, int ns, int* sl_ptr, long long* total) {
+  __shared__ long long sh[1024];
+  const int t = threadIdx.x, per = (ns + 1023) / 1024;
+  const int a = min(ns, t * per), b = min(ns, a + per);
+  long long s = 0;
+  for (int i = a; i < b; i++) s += 32ll * width[i];
+  sh[t] = s;
+  __syncthreads();
+  for (int d = 1; d < 1024; d <<= 1) {  // inclusive scan (Hillis-Steele)
+    const long long v = t >= d ? sh[t - d] : 0;
+    __syncthreads();
+    sh[t] += v;
+    __syncthreads();
+  }
+  long long off = sh[t] - s;
+  for (int i = a; i < b; i++) {
+    sl_ptr[i] = int(min(off, 0x7fffffffll));
+    off += 32ll * width[i];
+  }
+  if (t == 1023) {
+    sl_ptr[ns] = int(min(sh[1023], 0x7fffffffll));
+    *total = sh[1023];
+  }
+}
+// SELL entries from CSR, one warp per slice: entry k of slot l at
+// sl_ptr[s] + 32 k + l; short rows padded with their own column and 0.
+template <class SV, class DV>
+__global__ void sell_fill(CgMat S, const int* rp, const int* ci, const SV* val, int* eci, DV* ev) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < S.nslices; s += nwarps) {
+    const int e0 = S.sl_ptr[s], w = (S.sl_ptr[s + 1] - e0) >> 5;
+    const int row = S.sl_row[s * 32 + lane];
+    const bool real = row < S.n;
+    const int j0 = real ? rp[row] : 0, len = real ? rp[row + 1] - j0 : 0;
+    for (int k = 0; k < w; k++) {
+      const int e = e0 + 32 * k + lane;
+      eci[e] = k < len ? ci[j0 + k] : (real ? row : 0);
+      ev[e] = k < len ? DV(val[j0 + k]) : DV(0);
+    }
+  }
+}
+
 __global__ void to_f32(const double* src, size_t n, float* dst) {
   for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
     dst[i] = float(src[i]);
@@ -1174,6 +1309,55 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
       if (mixed) P.val32 = static_cast<float*>(ev);
     }
   }
+  if (A.fmt == 0 && o->kernel == PERKS_KERNEL_PERSISTENT && n > 0 && P.A.fmt == 0) {
+    // Irregular CSR: SELL-32 copy with rows sorted by length within windows,
+    // kept when its padding stays below 30% of the entries
+    const int nwin = (n + kSellWindow - 1) / kSellWindow, ns = nwin * (kSellWindow / 32);
+    const size_t rows_b = (size_t(ns) * 32 * 4 + 255) & ~size_t(255);
+    const size_t wid_b = (size_t(ns) * 4 + 255) & ~size_t(255);
+    const size_t ptr_b = (size_t(ns + 1) * 4 + 255) & ~size_t(255);
+    unsigned char* mw = static_cast<unsigned char*>(workspace(kWsCgSell, rows_b + wid_b + ptr_b + 256, &st));
+    if (!mw) return st;
+    int* sl_row = reinterpret_cast<int*>(mw);
+    int* width = reinterpret_cast<int*>(mw + rows_b);
+    int* sl_ptr = reinterpret_cast<int*>(mw + rows_b + wid_b);
+    long long* tot = reinterpret_cast<long long*>(mw + rows_b + wid_b + ptr_b);
+    sell_sort<<<nwin, kSellWindow, 0, s>>>(A.rp, n, sl_row, width);
+    sell_scan<<<1, 1024, 0, s>>>(width, ns, sl_ptr, tot);
+    long long total = 0;
+    PERKS_CUDA(cudaMemcpyAsync(&total, tot, sizeof(total), cudaMemcpyDeviceToHost, s));
+    PERKS_CUDA(cudaStreamSynchronize(s));
+    count_launch(2);
+    if (total < 0x7fffffffll && 10 * total <= 13ll * std::max(A.nnz, 1)) {
+      const size_t evb = (f32 || mixed) ? 4 : 8;
+      const size_t ci_bytes = (size_t(total) * 4 + 255) & ~size_t(255);
+      unsigned char* m = static_cast<unsigned char*>(workspace(kWsCgMat, ci_bytes + size_t(total) * evb + 16, &st));
+      if (!m) return st;
+      int* eci = reinterpret_cast<int*>(m);
+      void* ev = m + ci_bytes;
+      CgMat S = A;
+      S.fmt = 3;
+      S.eci = eci;
+      S.sl_ptr = sl_ptr;
+      S.sl_row = sl_row;
+      S.nslices = ns;
+      const int g = dev->sms * 8;
+      if (f32)
+        sell_fill<float, float><<<g, 256, 0, s>>>(S, A.rp, A.ci, static_cast<const float*>(A.val), eci,
+                                                   static_cast<float*>(ev));
+      else if (mixed)
+        sell_fill<double, float><<<g, 256, 0, s>>>(S, A.rp, A.ci, static_cast<const double*>(A.val), eci,
+                                                    static_cast<float*>(ev));
+      else
+        sell_fill<double, double><<<g, 256, 0, s>>>(S, A.rp, A.ci, static_cast<const double*>(A.val), eci,
+                                                     static_cast<double*>(ev));
+      PERKS_CUDA(cudaGetLastError());
+      count_launch(1);
+      S.val = mixed ? nullptr : ev;
+      P.A = S;
+      if (mixed) P.val32 = static_cast<float*>(ev);
+    }
+  }
   if (A.fmt == 0) {  // CSR SpMV: lanes per row, about half the mean row length
     const long long avg = (A.nnz + std::max(n, 1) - 1) / std::max(n, 1);
     int g = 4;
@@ -1191,7 +1375,7 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   // (DIA, ELL) alternate two buffers (iteration k writes P.p[k & 1]); the
   // others keep p in P.p[0]
   auto p_of = [&](int k) {
-    return (f32 && o->kernel == PERKS_KERNEL_PERSISTENT && P.A.fmt != 0) ? P.p[k & 1] : P.p[0];
+    return (f32 && o->kernel == PERKS_KERNEL_PERSISTENT && P.A.fmt != 0 && P.A.fmt != 3) ? P.p[k & 1] : P.p[0];
   };
   if (resume) {
     PERKS_CUDA(cudaMemcpyAsync(P.r, ck->d_r, size_t(n) * ws, cudaMemcpyDeviceToDevice, s));
@@ -1204,11 +1388,12 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
         o->dtype == PERKS_MIXED
             ? (f == 0 ? (const void*)cg_mixed<0, 0>
                : f == 2 ? (const void*)cg_mixed<2, 0>
+               : f == 3 ? (const void*)cg_mixed<3, 0>
                : A.fmt == 1 ? (const void*)cg_mixed<1, 1> : (const void*)cg_mixed<1, 0>)
         : f32 ? (f == 0 ? (const void*)cg_persistent<float, 0> : f == 1 ? (const void*)cg_persistent<float, 1>
-                                                                 : (const void*)cg_persistent<float, 2>)
+                 : f == 2 ? (const void*)cg_persistent<float, 2> : (const void*)cg_persistent<float, 3>)
               : (f == 0 ? (const void*)cg_persistent<double, 0> : f == 1 ? (const void*)cg_persistent<double, 1>
-                                                                  : (const void*)cg_persistent<double, 2>);
+                 : f == 2 ? (const void*)cg_persistent<double, 2> : (const void*)cg_persistent<double, 3>);
     int per_sm = 0;
     PERKS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCgThreads, 0));
     if (per_sm < 1) return fail(PERKS_ERR_LAUNCH, "CG kernel does not fit on an SM");
@@ -1318,6 +1503,7 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
     res->true_rel_res = tr[1] > 0 ? std::sqrt(tr[0] / tr[1]) : std::sqrt(tr[0]);
     res->ms = ms;
     res->launches = launches;
+    res->layout = P.A.fmt;
   }
   const double thr = o->stop == PERKS_STOP_REL ? o->tol * o->tol * tr[1] : o->tol * o->tol;
   if (!o->static_iter && iters >= o->max_iter && !(rr < thr))

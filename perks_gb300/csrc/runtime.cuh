@@ -32,7 +32,7 @@ const DeviceInfo* device_info();
 
 // Grow-only per-device scratch buffers, keyed by slot. Not thread-safe (the
 // reference API is single-threaded too). Returned memory is not cleared.
-enum WorkSlot { kWsField0 = 0, kWsField1, kWsSync, kWsCgVec, kWsCgScalar, kWsCgMat, kWsSlots };
+enum WorkSlot { kWsField0 = 0, kWsField1, kWsSync, kWsCgVec, kWsCgScalar, kWsCgMat, kWsCgSell, kWsSlots };
 void* workspace(WorkSlot slot, size_t bytes, int* status);
 
 void count_launch(int n = 1);

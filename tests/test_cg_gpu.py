@@ -141,22 +141,51 @@ def _shuffled_columns(rp, ci, v, seed):
     return rp, ci2, v2
 
 
-# CSR layouts the persistent solver chooses internally: diagonal structure
-# (sorted columns, few diagonals: solved as DIA), bounded rows on scattered
-# diagonals (ELL copy), unsorted columns (ELL copy: the DIA copy needs sorted
-# columns), long irregular rows (CSR as given).
-@pytest.mark.parametrize("layout", ["diagonals", "scattered", "unsorted", "irregular"])
-@pytest.mark.parametrize("dtype", ["fp64", "mixed"])
-def test_cg_csr_layouts(native, cuda, oracle, layout, dtype):
+def _arrow(n, seed):
+    """Arrowhead SPD matrix: a tridiagonal band plus a dense first row and
+    column (row 0 holds n entries), diagonally dominant."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    off = rng.uniform(-1, 0, n - 1)
+    arm = rng.uniform(-1, 1, n - 1) * 0.01
+    A = sp.diags([off, off], [-1, 1], shape=(n, n)).tolil()
+    A[0, 1:] = arm
+    A[1:, 0] = arm[:, None]
+    A = A.tocsr()
+    d = np.abs(A).sum(axis=1).A1 + rng.uniform(0.1, 1.0, n)
+    A = (A + sp.diags(d)).tocsr()
+    A.sort_indices()
+    return A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data
+
+
+# CSR layouts the persistent solver chooses internally (perks_cg_result
+# .layout): diagonal structure (sorted columns, few diagonals: DIA copy, 1),
+# bounded rows on scattered diagonals (ELL copy, 2), unsorted columns (ELL:
+# the DIA copy needs sorted columns), irregular rows of 3..60 entries (SELL
+# copy, 3), and one dense row among short ones (SELL padding too large: CSR
+# as given, lane groups, 0).
+@pytest.mark.parametrize("layout,expect", [("diagonals", 1), ("scattered", 2), ("unsorted", 2), ("irregular", 3),
+                                           ("arrow", 0)])
+@pytest.mark.parametrize("dtype", ["fp64", "mixed", "fp32"])
+def test_cg_csr_layouts(native, cuda, oracle, layout, expect, dtype):
     pytest.importorskip("scipy")
     from perks_gb300 import matrices as M
     base = M.laplacian_2d(96)
     rp, ci, v = {"diagonals": lambda: base, "scattered": lambda: _permuted(*base, seed=3),
                  "unsorted": lambda: _shuffled_columns(*base, seed=4),
-                 "irregular": lambda: M.random_spd(20000, 5)}[layout]()
+                 "irregular": lambda: M.random_spd(20000, 5), "arrow": lambda: _arrow(20000, 6)}[layout]()
     b = np.random.default_rng(6).uniform(-1, 1, len(rp) - 1)
     _, it, _, _ = oracle.cg(rp, ci, v, b, max_iter=20000, stop=1, tol=1e-10)
+    if dtype == "fp32":
+        # the reference's float build: tracks the float oracle for a few iterations
+        v32, b32 = v.astype(np.float32), b.astype(np.float32)
+        xo, _, _, _ = oracle.cg(rp, ci, v32, b32, max_iter=8, static_iter=True)
+        x, res = native.cg_csr(rp, ci, v32, b32, dtype="fp32", max_iter=8, static_iter=True, device=cuda)
+        assert res["layout"] == expect
+        assert np.allclose(x.cpu().numpy(), xo, rtol=2e-4, atol=1e-5)
+        return
     x, res = native.cg_csr(rp, ci, v, b, dtype=dtype, tol=1e-10, device=cuda)
+    assert res["layout"] == expect, res
     if dtype == "fp64":
         assert it_close(res["iterations"], it), (layout, res, it)
     assert res["true_rel_res"] <= 1e-10 * 1.05

@@ -73,7 +73,7 @@ def test_batch_job_barrier_timeout(native, cuda, oracle):
     import torch
     from perks_gb300.batch import BatchPlan, stencil_job
     f = np.random.default_rng(5).random((600, 900))
-    small = np.random.default_rng(6).random((40, 50))
+    small = np.random.default_rng(6).random((16, 16))  # far below the slicing unit: one work item
     ta, ts = torch.from_numpy(f).to(cuda), torch.from_numpy(small).to(cuda)
     oa, os_ = torch.empty_like(ta), torch.empty_like(ts)
     jobs = [stencil_job(ta, oa, "2d5pt", 5), stencil_job(ts, os_, "2d5pt", 5)]

@@ -78,5 +78,6 @@ def test_noalloc_allocates_nothing(native, cuda):
     # every buffer of the calls exists before free0 is read, so the device's
     # free memory only moves if the entry point allocated something
     assert free1 == free0, (free0, free1)
-    ref, _ = _call(native, "perks_stencil2d", big, "2ds9pt", 1)
+    rc, ref = _call(native, "perks_stencil2d", big, "2ds9pt", 1)
+    assert rc == 0, native.last_error()
     assert torch.equal(ref.view(torch.uint8), out_big.view(torch.uint8))
