@@ -541,10 +541,13 @@ def cg_summary(res, bytes_per_iter=None):
 
 def extra_batch(P, torch, n_jobs=512, steps=100, seed=42):
     """The batched uneven workload (perks_gb300.batch.synthetic_workload: 512
-    instances of 2D/3D stencils and shifted-Laplacian CG, FP32/FP64) in one
-    persistent launch (a CUDA graph, autotuned launch shape), against every
-    instance run alone through the single-instance entry points (sum of their
-    device times)."""
+    instances of 2D/3D stencils in FP32/FP64 storage and shifted-Laplacian
+    CG in FP64/mixed precision, every CG job to 1e-10) in one persistent
+    launch (a CUDA graph, autotuned launch shape), against every instance run
+    alone through the single-instance entry points in the same precisions,
+    and against the plain FP64 path (every instance alone in FP64); sums of
+    device times. The CG jobs' true relative residuals are recomputed on the
+    host in FP64 (worst one reported)."""
     from perks_gb300.batch import BatchPlan, synthetic_workload
     jobs, alone = synthetic_workload(n_jobs, steps, seed)
     with BatchPlan(jobs) as plan:
@@ -553,19 +556,34 @@ def extra_batch(P, torch, n_jobs=512, steps=100, seed=42):
         res = plan.results()
     st = min(runs, key=lambda r: r["ms"])
     bad = sum(1 for r in res if r["status"] != 0)
-    alone_ms = 0.0
+    import numpy as np
+    worst = 0.0
+    for j, a in zip(jobs, alone):
+        if a[0] == "cg":
+            rp, ci, v, b = a[1]
+            xs = j["x"].double().cpu().numpy()
+            r = b - (np.add.reduceat(v * xs[ci], rp[:-1]) if len(ci) else 0.0)
+            worst = max(worst, float(np.linalg.norm(r) / np.linalg.norm(b)))
+    alone_ms, fp64_ms = 0.0, 0.0
     for a in alone:
         if a[0] == "stencil":
             fn = P.stencil2d if a[1].dim() == 2 else P.stencil3d
             _, s1 = fn(a[1], a[2], steps)
             alone_ms += s1["ms"]
+            _, s2 = fn(a[1].double(), a[2], steps) if a[1].dtype != torch.float64 else (None, s1)
+            fp64_ms += s2["ms"]
         else:
             rp, ci, v, b = a[1]
             _, r1 = P.cg_csr(rp, ci, v, b, dtype=a[2], tol=a[3], max_iter=20000, check=False)
             alone_ms += r1["ms"]
+            if a[2] != "fp64":
+                _, r1 = P.cg_csr(rp, ci, v, b, dtype="fp64", tol=a[3], max_iter=20000, check=False)
+            fp64_ms += r1["ms"]
     torch.cuda.synchronize()
     return {"batch_512": {"jobs": n_jobs, "batch_ms": round(st["ms"], 2), "alone_ms_sum": round(alone_ms, 2),
-                          "speedup": round(alone_ms / st["ms"], 2), "threads": st["threads"],
+                          "speedup": round(alone_ms / st["ms"], 2), "plain_fp64_alone_ms_sum": round(fp64_ms, 2),
+                          "speedup_vs_plain_fp64": round(fp64_ms / st["ms"], 2),
+                          "cg_worst_true_rel_res": worst, "threads": st["threads"],
                           "ctas_per_sm": st["ctas_per_sm"], "resident_stencil_jobs": st["resident_jobs"],
                           "sliced_stencil_jobs": st["sliced_jobs"], "jobs_not_ok": bad}}
 

@@ -190,14 +190,22 @@ typedef enum {
  * solve can stop and later resume exactly where it stopped (the resumed run
  * gives bit-identical x and r to one uninterrupted run with the same options).
  * The caller owns d_r and d_p (n elements of the working type: FP64 for
- * PERKS_FP64, FP32 for PERKS_FP32); the solution itself is the caller's x.
- * Not available for PERKS_MIXED. */
+ * PERKS_FP64, FP32 for PERKS_FP32 and PERKS_MIXED) and, for PERKS_MIXED, d_xs
+ * (n floats); the solution itself is the caller's x. A mixed-precision solve
+ * given a checkpoint keeps the increment that its last iterations built in
+ * d_xs instead of adding it to x when it stops at max_iter, so that the
+ * resumed solve continues exactly as an uninterrupted one: x + d_xs is then
+ * the iterate. */
 typedef struct {
-  void* d_r;        /* device: residual r */
+  void* d_r;        /* device: residual r (PERKS_MIXED: the FP32 recursive residual) */
   void* d_p;        /* device: the last search direction p */
+  void* d_xs;       /* device, PERKS_MIXED only: the FP32 solution increment not yet added to x */
   double rr;        /* r.r as the iteration holds it (in the working precision) */
   double rr_prev;   /* r.r one iteration earlier (for beta) */
   double bb;        /* b.b (relative stop) */
+  double maxrr;     /* PERKS_MIXED: r.r at the last reliable update */
+  int outer;        /* PERKS_MIXED: reliable updates done */
+  int since;        /* PERKS_MIXED: iterations since the last reliable update */
   int k;            /* iterations completed; 0 = no state yet (start from x) */
   int kernel;       /* perks_kernel that wrote the state; resuming needs the same */
   int dtype;        /* perks_dtype that wrote the state; resuming needs the same */
@@ -221,6 +229,12 @@ typedef struct {
                                  writes its final state back, also when it returns
                                  PERKS_ERR_NOT_CONVERGED. max_iter counts all iterations,
                                  including those before the checkpoint. */
+  int cache_vectors;  /* persistent kernel: KB of shared memory per CTA in which each CTA keeps its
+                         rows of the vectors that only it touches (r unless the SpMV gathers it, x
+                         or the mixed increment, Ap) for the whole solve; the rest streams.
+                         0 = none, -1 = the library's default (none: the shared memory is taken
+                         from the L1 cache that the SpMV gathers use, and on GB300 that cost more
+                         than it saved) */
 } perks_cg_opts;
 
 typedef struct {
@@ -274,7 +288,8 @@ typedef enum { PERKS_JOB_STENCIL = 0, PERKS_JOB_CG = 1 } perks_job_kind;
 
 typedef struct {
   int kind;          /* perks_job_kind */
-  int dtype;         /* PERKS_FP32 or PERKS_FP64 */
+  int dtype;         /* PERKS_FP32 or PERKS_FP64; CG jobs also PERKS_MIXED (FP64 values, b and x, FP32
+                        inner iteration with FP64 reliable updates, for FP64 tolerances) */
   /* stencil: shape (PERKS_2D5PT, PERKS_2DS9PT, PERKS_2D9PT or PERKS_3D7PT),
    * clamp boundary, reference evaluation order; h = 1 for 2D */
   int shape, h, wy, wx, steps;

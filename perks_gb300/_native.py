@@ -46,14 +46,15 @@ class StencilStats(ctypes.Structure):
 
 
 class CgState(ctypes.Structure):
-    _fields_ = [("d_r", c_void_p), ("d_p", c_void_p), ("rr", c_double), ("rr_prev", c_double),
-                ("bb", c_double), ("k", c_int), ("kernel", c_int), ("dtype", c_int), ("n", c_int)]
+    _fields_ = [("d_r", c_void_p), ("d_p", c_void_p), ("d_xs", c_void_p), ("rr", c_double), ("rr_prev", c_double),
+                ("bb", c_double), ("maxrr", c_double), ("outer", c_int), ("since", c_int), ("k", c_int),
+                ("kernel", c_int), ("dtype", c_int), ("n", c_int)]
 
 
 class CgOpts(ctypes.Structure):
     _fields_ = [("dtype", c_int), ("stop", c_int), ("tol", c_double), ("max_iter", c_int),
                 ("static_iter", c_int), ("kernel", c_int), ("replace_every", c_int), ("ctas", c_int),
-                ("stream", c_void_p), ("checkpoint", ctypes.POINTER(CgState))]
+                ("stream", c_void_p), ("checkpoint", ctypes.POINTER(CgState)), ("cache_vectors", c_int)]
 
 
 class CgResult(ctypes.Structure):

@@ -35,10 +35,16 @@ def stencil_job(field_in, field_out, shape: str, steps: int) -> dict:
             "wx": wx, "steps": int(steps), "in": field_in.contiguous(), "out": field_out}
 
 
-def cg_job(row_ptr, col, val, b, x, tol: float = 1e-10, max_iter: int = 100000) -> dict:
+def cg_job(row_ptr, col, val, b, x, tol: float = 1e-10, max_iter: int = 100000, mixed: bool = False) -> dict:
     """CG on CSR device tensors (row_ptr, col int32; val, b, x of one float
-    dtype); x receives the solution (it starts from 0)."""
-    return {"kind": N.JOB_CG, "dtype": _dtype_code(val), "n": int(b.numel()), "nnz": int(col.numel()),
+    dtype); x receives the solution (it starts from 0). mixed=True (float64
+    tensors): FP32 inner iteration with FP64 reliable updates."""
+    dt = _dtype_code(val)
+    if mixed:
+        if dt != N.FP64:
+            raise TypeError("a mixed-precision job takes float64 values, b and x")
+        dt = N.MIXED
+    return {"kind": N.JOB_CG, "dtype": dt, "n": int(b.numel()), "nnz": int(col.numel()),
             "rp": row_ptr, "ci": col, "val": val, "b": b, "x": x, "tol": float(tol), "max_iter": int(max_iter)}
 
 
@@ -97,9 +103,11 @@ def synthetic_workload(n_jobs: int = 512, steps: int = 100, seed: int = 42, devi
     """The batched uneven workload of the benchmark: n_jobs instances, a third
     each of 2D 5/9-point stencils (64^2..1024^2, log-uniform), 3D 7-point
     stencils (32^3..128^3) and CG on 2D/3D Laplacians (n = 1e3..1e5,
-    log-uniform) with a diagonal shift U(0, 0.5); FP32 and FP64 alternating;
-    `steps` time steps per stencil; CG to 1e-10 (FP64) / 1e-5 (FP32). Seeded
-    uniform [0,1) fields and uniform [-1,1) right-hand sides.
+    log-uniform) with a diagonal shift U(0, 0.5); stencils in FP32 and FP64
+    storage alternating, CG in FP64 and mixed precision (FP32 inner
+    iteration, FP64 reliable updates) alternating, every CG job to the FP64
+    tolerance 1e-10; `steps` time steps per stencil. Seeded uniform [0,1)
+    fields and uniform [-1,1) right-hand sides.
 
     Returns (jobs, alone): the batch jobs, and per job what the
     single-instance path needs: ("stencil", field, shape) or
@@ -132,9 +140,10 @@ def synthetic_workload(n_jobs: int = 512, steps: int = 100, seed: int = 42, devi
                 rp, ci, v = M.laplacian_3d(max(4, int(round(nt ** (1 / 3)))))
             rp, ci, v = M.shifted(rp, ci, v, rng.uniform(0, 0.5))
             b = rng.uniform(-1, 1, len(rp) - 1)
-            tol = 1e-10 if dt == torch.float64 else 1e-5
+            mixed = dt == torch.float32
             t = lambda x, ty: torch.from_numpy(np.ascontiguousarray(x)).to(dev, ty)
-            x = torch.empty(len(b), dtype=dt, device=dev)
-            jobs.append(cg_job(t(rp, torch.int32), t(ci, torch.int32), t(v, dt), t(b, dt), x, tol=tol, max_iter=20000))
-            alone.append(("cg", (rp, ci, v, b), "fp64" if dt == torch.float64 else "fp32", tol))
+            x = torch.empty(len(b), dtype=torch.float64, device=dev)
+            jobs.append(cg_job(t(rp, torch.int32), t(ci, torch.int32), t(v, torch.float64), t(b, torch.float64), x,
+                               tol=1e-10, max_iter=20000, mixed=mixed))
+            alone.append(("cg", (rp, ci, v, b), "mixed" if mixed else "fp64", 1e-10))
     return jobs, alone

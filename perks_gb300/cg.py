@@ -27,35 +27,48 @@ def _dev(a, dtype, device):
 class CgCheckpoint:
     """CG iteration state between two iterations (perks_cg_state): residual r,
     last search direction p, r.r of the last two iterations, b.b and the
-    iteration count. Pass it as ``checkpoint=`` to cg_csr / cg_dia: a solve
-    resumes from it when it holds a state (k > 0; x0 must then be the
-    iterate saved with it) and leaves its final state in it. ``to_host`` /
-    ``from_host`` move it to numpy (for example to np.savez it with x)."""
+    iteration count; for mixed precision also the FP32 solution increment
+    x_s and the reliable-update bookkeeping. Pass it as ``checkpoint=`` to
+    cg_csr / cg_dia: a solve resumes from it when it holds a state (k > 0; x0
+    must then be the iterate saved with it) and leaves its final state in it.
+    ``to_host`` / ``from_host`` move it to numpy (for example to np.savez it
+    with x)."""
+
+    _SCALARS = ("rr", "rr_prev", "bb", "maxrr")
+    _INTS = ("outer", "since", "k", "kernel", "dtype", "n")
 
     def __init__(self):
         self.r = None
         self.p = None
+        self.xs = None
         self.state = N.CgState()
 
     @property
     def k(self) -> int:
         return self.state.k
 
-    def _bind(self, n, dtype, device):
+    def _bind(self, n, dtype, device, mixed=False):
         import torch
         if self.r is None:
             self.r = torch.zeros(n, dtype=dtype, device=device)
             self.p = torch.zeros(n, dtype=dtype, device=device)
         if self.r.numel() != n or self.r.dtype != dtype:
             raise ValueError("checkpoint holds a state of another size or dtype")
+        if mixed and self.xs is None:
+            self.xs = torch.zeros(n, dtype=torch.float32, device=device)
         self.state.d_r = self.r.data_ptr()
         self.state.d_p = self.p.data_ptr()
+        self.state.d_xs = self.xs.data_ptr() if self.xs is not None else None
         return ctypes.pointer(self.state)
 
     def to_host(self) -> dict:
         st = self.state
-        return {"r": self.r.cpu().numpy(), "p": self.p.cpu().numpy(), "rr": st.rr, "rr_prev": st.rr_prev,
-                "bb": st.bb, "k": st.k, "kernel": st.kernel, "dtype": st.dtype, "n": st.n}
+        d = {"r": self.r.cpu().numpy(), "p": self.p.cpu().numpy()}
+        if self.xs is not None:
+            d["xs"] = self.xs.cpu().numpy()
+        for f in self._SCALARS + self._INTS:
+            d[f] = getattr(st, f)
+        return d
 
     @classmethod
     def from_host(cls, d: dict, device="cuda") -> "CgCheckpoint":
@@ -63,17 +76,17 @@ class CgCheckpoint:
         c = cls()
         c.r = torch.from_numpy(np.ascontiguousarray(d["r"])).to(device)
         c.p = torch.from_numpy(np.ascontiguousarray(d["p"])).to(device)
-        for f in ("rr", "rr_prev", "bb"):
+        if "xs" in d:
+            c.xs = torch.from_numpy(np.ascontiguousarray(d["xs"])).to(device)
+        for f in cls._SCALARS:
             setattr(c.state, f, float(d[f]))
-        c.state.k = int(d["k"])
-        c.state.kernel = int(d["kernel"])
-        c.state.dtype = int(d["dtype"])
-        c.state.n = int(d["n"])
+        for f in cls._INTS:
+            setattr(c.state, f, int(d[f]))
         return c
 
 
 def _opts(dtype="fp64", stop="rel", tol=1e-10, max_iter=100000, static_iter=False, kernel="persistent",
-          replace_every=0, ctas=0, stream=None):
+          replace_every=0, ctas=0, stream=None, cache_vectors=-1):
     o = N.CgOpts()
     N.lib().perks_cg_default_opts(ctypes.byref(o))
     o.dtype = _DT[dtype]
@@ -85,6 +98,7 @@ def _opts(dtype="fp64", stop="rel", tol=1e-10, max_iter=100000, static_iter=Fals
     o.replace_every = int(replace_every)
     o.ctas = int(ctas)
     o.stream = stream
+    o.cache_vectors = int(cache_vectors)
     return o
 
 
@@ -108,7 +122,8 @@ def cg_csr(row_ptr, col, val, b, x0=None, *, dtype="fp64", device="cuda", check=
         kw["stream"] = ctypes.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
     o = _opts(dtype, **kw)
     if checkpoint is not None:
-        o.checkpoint = checkpoint._bind(n, vdt, x.device)
+        wdt = torch.float64 if dtype == "fp64" else torch.float32  # the iteration's working type
+        o.checkpoint = checkpoint._bind(n, wdt, x.device, mixed=dtype == "mixed")
     res = N.CgResult()
     rc = N.lib().perks_cg_csr(n, ci.numel(), rp.data_ptr(), ci.data_ptr(), v.data_ptr(), bb.data_ptr(),
                               x.data_ptr(), ctypes.byref(o), ctypes.byref(res))
@@ -132,7 +147,8 @@ def cg_dia(offsets, data, b, x0=None, *, dtype="fp64", device="cuda", check=True
         kw["stream"] = ctypes.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
     o = _opts(dtype, **kw)
     if checkpoint is not None:
-        o.checkpoint = checkpoint._bind(n, vdt, x.device)
+        wdt = torch.float64 if dtype == "fp64" else torch.float32  # the iteration's working type
+        o.checkpoint = checkpoint._bind(n, wdt, x.device, mixed=dtype == "mixed")
     res = N.CgResult()
     rc = N.lib().perks_cg_dia(n, len(off), off.ctypes.data, d.data_ptr(), bb.data_ptr(), x.data_ptr(),
                               ctypes.byref(o), ctypes.byref(res))

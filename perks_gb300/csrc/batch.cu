@@ -17,7 +17,10 @@
 //     global memory (L2-resident for these sizes). Clamp boundary, reference
 //     evaluation order: results are bit-identical to the single-instance path
 //     and to the reference CPU code.
-//   * CG job: CSR, x0 = 0, CTA-wide reductions, stop at ||r|| <= tol ||b||.
+//   * CG job: CSR, x0 = 0, CTA-wide reductions, stop at ||r|| <= tol ||b||;
+//     FP64, FP32, or mixed precision (the FP32 iteration with FP64 reliable
+//     updates of the single-instance solver, so that the job reaches an FP64
+//     tolerance).
 // A run is a CUDA graph of {reset the counter, launch}; the launch shape
 // (threads per CTA, CTAs per SM, hence shared memory per CTA) is chosen by
 // timing each candidate once when the plan is created.
@@ -241,6 +244,95 @@ __device__ void batch_cg(const BJob& J, double* red, BRes* res) {
   }
 }
 
+// Mixed-precision CG job in one CTA (the reliable-update scheme of the
+// single-instance cg_mixed: Sleijpen & van der Vorst 1996): the Krylov
+// iteration runs in FP32 on an FP32 copy of the values (products summed in
+// FP32 per row, dot products in FP64); the solution x is accumulated in FP64,
+// and whenever the recursive r.r has dropped by delta^2 = 0.01 since the last
+// update (or claims convergence, or the iteration cap is reached) x += x_s and
+// r = b - A x is recomputed with the FP64 values. Convergence is declared on
+// that FP64 true residual only. Scratch: FP32 r, p, Ap, x_s and the values.
+__device__ void batch_cg_mixed(const BJob& J, double* red, BRes* res) {
+  const int n = J.n, nt = blockDim.x, tid = threadIdx.x;
+  const int* __restrict__ rp = J.rp;
+  const int* __restrict__ ci = J.ci;
+  const double* __restrict__ val = static_cast<const double*>(J.val);
+  const double* __restrict__ b = static_cast<const double*>(J.b);
+  double* __restrict__ x = static_cast<double*>(J.x);
+  const size_t np = size_t((n + 63) & ~63);
+  float* __restrict__ r = static_cast<float*>(J.scratch);
+  float* __restrict__ p = r + np;
+  float* __restrict__ Ap = p + np;
+  float* __restrict__ xs = Ap + np;
+  float* __restrict__ v32 = xs + np;
+  for (int j = tid; j < J.nnz; j += nt) v32[j] = float(val[j]);
+  double rr = 0.0;
+  for (int i = tid; i < n; i += nt) {
+    const double bi = b[i];
+    x[i] = 0.0;
+    r[i] = float(bi);
+    xs[i] = 0.0f;
+    rr += bi * bi;
+  }
+  rr = cta_sum(rr, red);  // also orders the writes above before the reads below
+  const double bb = rr, stop2 = J.tol * J.tol * bb;
+  double maxrr = rr, rr0 = 0.0;
+  int k = 0, status = PERKS_OK;
+  while (k < J.max_iter && rr > stop2) {
+    const float beta = k > 0 ? float(rr / rr0) : 0.0f;
+    for (int i = tid; i < n; i += nt) p[i] = k > 0 ? fmaf(beta, p[i], r[i]) : r[i];
+    __syncthreads();  // p complete before the SpMV gathers it
+    double pap = 0.0;
+    for (int i = tid; i < n; i += nt) {
+      float acc = 0.0f;
+      for (int j = rp[i]; j < rp[i + 1]; j++) acc = fmaf(v32[j], p[ci[j]], acc);
+      Ap[i] = acc;
+      pap += double(p[i] * acc);
+    }
+    pap = cta_sum(pap, red);
+    if (!(pap > 0.0) || !isfinite(pap)) {
+      status = PERKS_ERR_BREAKDOWN;
+      break;
+    }
+    const float alpha = float(rr / pap);
+    double rrn = 0.0;
+    for (int i = tid; i < n; i += nt) {
+      xs[i] = fmaf(alpha, p[i], xs[i]);
+      const float ri = fmaf(-alpha, Ap[i], r[i]);
+      r[i] = ri;
+      rrn += double(ri * ri);
+    }
+    rrn = cta_sum(rrn, red);
+    k++;
+    if (rrn < 0.01 * maxrr || rrn <= stop2 || k == J.max_iter) {
+      // reliable update: x += x_s in FP64, true residual with the FP64 values
+      for (int i = tid; i < n; i += nt) {
+        x[i] += double(xs[i]);
+        xs[i] = 0.0f;
+      }
+      __syncthreads();  // x complete before the SpMV gathers it
+      double rt = 0.0;
+      for (int i = tid; i < n; i += nt) {
+        double acc = 0.0;
+        for (int j = rp[i]; j < rp[i + 1]; j++) acc = fma(val[j], x[ci[j]], acc);
+        const double ri = b[i] - acc;
+        r[i] = float(ri);
+        rt += ri * ri;
+      }
+      rrn = cta_sum(rt, red);
+      maxrr = rrn;
+    }
+    rr0 = rr;
+    rr = rrn;
+  }
+  if (status == PERKS_OK && rr > stop2) status = PERKS_ERR_NOT_CONVERGED;
+  if (tid == 0) {
+    res->iterations = k;
+    res->status = status;
+    res->rel_res = bb > 0.0 ? sqrt(rr / bb) : sqrt(rr);
+  }
+}
+
 // counter[0]: the queue; counter[1 + job]: the job barriers (all zero at launch)
 __global__ void __launch_bounds__(1024, 1)
     batch_kernel(const BJob* __restrict__ jobs, const BItem* __restrict__ items, int nitems, BRes* res,
@@ -278,7 +370,8 @@ __global__ void __launch_bounds__(1024, 1)
           break;
       }
     } else if (J.kind == PERKS_JOB_CG) {
-      if (f64) batch_cg<double>(J, red, res + j);
+      if (J.dtype == PERKS_MIXED) batch_cg_mixed(J, red, res + j);
+      else if (f64) batch_cg<double>(J, red, res + j);
       else batch_cg<float>(J, red, res + j);
     } else {
       switch (J.shape) {
@@ -398,7 +491,9 @@ int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_
   for (int i = 0; i < njobs; i++) {
     const perks_job& J = jobs[i];
     const std::string at = "job " + std::to_string(i) + ": ";
-    if (J.dtype != PERKS_FP32 && J.dtype != PERKS_FP64) return fail(PERKS_ERR_INVALID_ARG, at + "dtype");
+    const bool mixed = J.dtype == PERKS_MIXED;
+    if (J.dtype != PERKS_FP32 && J.dtype != PERKS_FP64 && !(mixed && J.kind == PERKS_JOB_CG))
+      return fail(PERKS_ERR_INVALID_ARG, at + "dtype (PERKS_MIXED is for CG jobs)");
     const size_t es = J.dtype == PERKS_FP64 ? 8 : 4;
     if (J.kind == PERKS_JOB_STENCIL) {
       if (!batch_shape_ok(J.shape))
@@ -416,7 +511,10 @@ int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_
         return fail(PERKS_ERR_INVALID_ARG, at + "bad CSR arguments");
       if (J.max_iter < 0 || !(J.tol >= 0)) return fail(PERKS_ERR_INVALID_ARG, at + "bad max_iter or tol");
       cost[i] = double(J.nnz + J.n) * std::sqrt(double(J.n)) * 4.0 * (J.dtype == PERKS_FP64 ? 4.0 : 1.0);
-      scratch_bytes[i] = 3 * ((size_t((J.n + 63) & ~63) * es + 255) & ~size_t(255));
+      // FP64/FP32: r, p, Ap; mixed: FP32 r, p, Ap, x_s (the vectors of 64-row
+      // multiples, one after another) and the FP32 values
+      scratch_bytes[i] = mixed ? ((size_t((J.n + 63) & ~63) * 16 + size_t(J.nnz) * 4 + 255) & ~size_t(255))
+                               : 3 * ((size_t((J.n + 63) & ~63) * es + 255) & ~size_t(255));
     } else {
       return fail(PERKS_ERR_INVALID_ARG, at + "unknown job kind");
     }

@@ -87,7 +87,6 @@ struct CgParams {
   void* Ap;
   // mixed precision extras
   float* val32;           // FP32 copy of the matrix values, in A's layout (built before the launch)
-  double* r64;            // FP64 true residual
   float* xs;              // FP32 solution increment
   double* part;           // [4][gridDim] partial sums
   double tol;
@@ -96,28 +95,24 @@ struct CgParams {
   int* out_iter;          // iterations done
   int* out_outer;         // reliable updates done
   double* out_rr;         // final r.r, then r.r one iteration earlier, then b.b
+  // rows per CTA kept in shared memory for the whole solve (multiples of 4;
+  // 0 = streamed): r (or, mixed, its FP32 r), x (mixed: x_s), Ap
+  int cap_r, cap_x, cap_ap;
   // resume from a checkpoint: r and p already in place, scalars here
   int resume, k0;         // k0 = iterations completed before this launch
   double rr0, rrp0, bb0;
+  double maxrr0;          // mixed: r.r at the last reliable update
+  int outer0, since0;     // mixed: reliable updates done, iterations since the last one
+  int keep_state;         // a checkpoint takes the final state
   unsigned* bar;
   unsigned* status;
   WaitCtl ctl;
 };
 
-// Merge-path split: first row of CTA `c` such that row + row_ptr[row] >= c*(n+nnz)/ncta.
-__device__ __forceinline__ int cg_split(const CgMat& A, int c, int ncta) {
-  if (A.fmt != 0) return int((long long)A.n * c / ncta);
-  const long long target = (long long)(A.n + (long long)A.nnz) * c / ncta;
-  int lo = 0, hi = A.n;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if ((long long)mid + A.rp[mid] < target) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-
-// SELL: first slice of CTA `c`, splitting slices + their padded entries evenly.
+// SELL: first slice of CTA `c`, splitting the slices by their padded
+// entries + rows. The SpMV of a CTA then writes rows that other CTAs own in
+// the row-wise phases (those are split evenly), so r and Ap of a SELL solve
+// stay in global memory.
 __device__ __forceinline__ int sell_split(const CgMat& A, int c, int ncta) {
   const long long total = (long long)A.sl_ptr[A.nslices] + 32ll * A.nslices;
   const long long target = total * c / ncta;
@@ -125,6 +120,20 @@ __device__ __forceinline__ int sell_split(const CgMat& A, int c, int ncta) {
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;
     if ((long long)A.sl_ptr[mid] + 32ll * mid < target) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// First row of CTA `c` in the row-wise phases: CSR by a merge-path split
+// (row + row_ptr[row] >= c*(n+nnz)/ncta), the other layouts evenly.
+__device__ __forceinline__ int cg_split(const CgMat& A, int c, int ncta) {
+  if (A.fmt != 0) return int((long long)A.n * c / ncta);
+  const long long target = (long long)(A.n + (long long)A.nnz) * c / ncta;
+  int lo = 0, hi = A.n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if ((long long)mid + A.rp[mid] < target) lo = mid + 1;
     else hi = mid;
   }
   return lo;
@@ -142,8 +151,25 @@ __device__ __forceinline__ void sell_rows(const CgMat& A, const MV* __restrict__
     const int e0 = __ldg(A.sl_ptr + s), e1 = __ldg(A.sl_ptr + s + 1);
     const int row = __ldg(A.sl_row + s * 32 + lane);
     XV acc = XV(0);
-#pragma unroll 4
-    for (int e = e0 + lane; e < e1; e += 32) acc = fma(XV(__ldg(val + e)), xv(__ldg(A.eci + e)), acc);
+    // batches of U entries: all column and value loads, then all gathers,
+    // then the multiply-adds in entry order (the chain column -> x -> fma
+    // would otherwise leave one gather per lane in flight)
+    constexpr int U = 8;
+    int e = e0 + lane;
+    for (; e + 32 * (U - 1) < e1; e += 32 * U) {
+      int c[U];
+      MV a[U];
+      XV g[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) c[u] = __ldg(A.eci + e + 32 * u);
+#pragma unroll
+      for (int u = 0; u < U; u++) a[u] = __ldg(val + e + 32 * u);
+#pragma unroll
+      for (int u = 0; u < U; u++) g[u] = xv(c[u]);
+#pragma unroll
+      for (int u = 0; u < U; u++) acc = fma(XV(a[u]), g[u], acc);
+    }
+    for (; e < e1; e += 32) acc = fma(XV(__ldg(val + e)), xv(__ldg(A.eci + e)), acc);
     if (row < A.n) epi(row, acc);
   }
 }
@@ -474,49 +500,92 @@ __device__ __forceinline__ void spmv4(const CgMat& A, const MV* __restrict__ val
   }
 }
 
+// A vector of which this CTA reads and writes only its own rows (never
+// gathered by another CTA): rows [base, cut) live in shared memory for the
+// whole solve, the rest in global memory (PERKS: the CTA's share of the
+// domain stays on chip across iterations and only the remainder streams).
+// base = row0 rounded down to 4 and cut - base is a multiple of 4, so a
+// four-row group is entirely on one side and 16-byte aligned there.
+template <class T>
+struct RowVec {
+  T* g;
+  T* s;
+  int base, cut;
+  __device__ __forceinline__ T* at(int i) const { return i < cut ? s + (i - base) : g + i; }
+  // global -> shared (rows [lo, hi) of the CTA), or back
+  __device__ __forceinline__ void load(int lo, int hi) const {
+    for (int i = lo + threadIdx.x; i < min(hi, cut); i += blockDim.x) s[i - base] = g[i];
+  }
+  __device__ __forceinline__ void store(int lo, int hi) const {
+    for (int i = lo + threadIdx.x; i < min(hi, cut); i += blockDim.x) g[i] = s[i - base];
+  }
+};
+// Shared-memory rows of the resident vectors, in the order of `caps` (rows,
+// multiples of 4; 0 = not resident). Dynamic shared memory of the CG kernels.
+extern __shared__ __align__(16) unsigned char cg_smem[];
+template <class T>
+__device__ __forceinline__ RowVec<T> row_vec(T* g, int cap, int row0, int row1, int& off) {
+  const int base = row0 & ~3;
+  const int span = (row1 - base + 3) & ~3;
+  RowVec<T> v{g, reinterpret_cast<T*>(cg_smem) + off, base, base + min(cap, max(span, 0))};
+  off += cap;
+  return v;
+}
+
 // Plain CG in one precision T (double, or float with the reference's float
-// build rounding of the scalars r.r, p.Ap, alpha and beta).
+// build rounding of the scalars r.r, p.Ap, alpha and beta). Vectors that
+// only the owning CTA touches (r unless the SpMV gathers it, x, Ap) keep the
+// CTA's rows in shared memory as far as P.cap_* allow.
 template <class T, int FMT>
 __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_constant__ CgParams P) {
-  // FP32 forms p where the SpMV gathers it, except for CSR: there the random
-  // gathers dominate, and gathering p_old and r instead of p doubles them
+  // FP32 forms p where the SpMV gathers it, except for CSR/SELL: there the
+  // random gathers dominate, and gathering p_old and r instead of p doubles
+  // them. Then r is gathered and stays in global memory.
   constexpr bool FUSE = sizeof(T) == 4 && FMT != 0 && FMT != 3;
   const CgMat& A = P.A;
   const T* __restrict__ val = static_cast<const T*>(A.val);
   const T* __restrict__ b = static_cast<const T*>(P.b);
-  T* __restrict__ x = static_cast<T*>(P.x);
-  T* __restrict__ r = static_cast<T*>(P.r);
-  T* __restrict__ Ap = static_cast<T*>(P.Ap);
+  T* __restrict__ r = static_cast<T*>(P.r);  // global r (gathered when FUSE)
   const int G = gridDim.x;
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
   const int2 sr = cta_slices<FMT>(A);
   GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G), P.ctl}};
   const int tid = threadIdx.x, nt = blockDim.x;
-  const bool xvec = aligned16(x);  // the caller's solution vector
+  const bool xvec = aligned16(P.x);  // the caller's solution vector
   const bool v4 = A.fmt != 0 && (A.n & 3) == 0 && aligned16(val) && aligned16(A.eci);  // DIA/ELL columns 16-byte aligned
+  int off = 0;
+  // SELL: the SpMV writes rows of other CTAs (r at the start, Ap): global
+  const RowVec<T> R = row_vec<T>(r, (FUSE || FMT == 3) ? 0 : P.cap_r, row0, row1, off);
+  const RowVec<T> X = row_vec<T>(static_cast<T*>(P.x), P.cap_x, row0, row1, off);
+  const RowVec<T> AP = row_vec<T>(static_cast<T*>(P.Ap), FMT == 3 ? 0 : P.cap_ap, row0, row1, off);
+  X.load(row0, row1);
 
   T r1, r0;
   double bb;
   int k;
   if (P.resume) {  // r and the last p were restored by the host
+    R.load(row0, row1);
+    __syncthreads();
     r1 = T(P.rr0);
     r0 = T(P.rrp0);
     bb = P.bb0;
     k = P.k0 + 1;
   } else {
+    __syncthreads();  // x in shared memory
     // r = b - A x ; rr = r.r ; bb = b.b  (per-thread sums in T, then double)
     T rr_t = T(0), bb_t = T(0);
     auto init_row = [&](int i, T ax) {
       const T bi = b[i];
       const T ri = T(-1) * ax + bi;
-      r[i] = ri;
+      *R.at(i) = ri;
       rr_t = fma(ri, ri, rr_t);
       bb_t = fma(bi, bi, bb_t);
     };
+    const T* __restrict__ xg = static_cast<const T*>(P.x);  // gathered: the global copy (x0)
     if constexpr (FMT == 3) {
-      sell_rows<T>(A, val, sr.x, sr.y, [x](int c) { return x[c]; }, init_row);
+      sell_rows<T>(A, val, sr.x, sr.y, [xg](int c) { return xg[c]; }, init_row);
     } else {
-      CG_ROWS(i, { init_row(i, spmv_row<FMT>(A, val, x, i)); })
+      CG_ROWS(i, { init_row(i, spmv_row<FMT>(A, val, xg, i)); })
     }
     double rr = double(rr_t);
     bb = double(bb_t);
@@ -552,11 +621,11 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
             pap_t = fma(pv[u], av[u], pap_t);
           }
           st4(p + i, pv);
-          st4(Ap + i, av);
+          st4(AP.at(i), av);
         }, [&](int i, T api) {
           const T pi = fma(beta, po[i], r[i]);
           p[i] = pi;
-          Ap[i] = api;
+          *AP.at(i) = api;
           pap_t = fma(pi, api, pap_t);
         });
       } else {
@@ -568,11 +637,11 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
 #pragma unroll
           for (int u = 0; u < 4; u++) pap_t = fma(rv[u], av[u], pap_t);
           st4(p + i, rv);
-          st4(Ap + i, av);
+          st4(AP.at(i), av);
         }, [&](int i, T api) {
           const T pi = r[i];
           p[i] = pi;
-          Ap[i] = api;
+          *AP.at(i) = api;
           pap_t = fma(pi, api, pap_t);
         });
       }
@@ -582,17 +651,17 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
         cg_rows4(row0, row1, true, [&](int i) {
           T pv[4], rv[4];
           ld4(p + i, pv);
-          ld4(r + i, rv);
+          ld4(R.at(i), rv);
 #pragma unroll
           for (int u = 0; u < 4; u++) pv[u] = fma(beta, pv[u], rv[u]);
           st4(p + i, pv);
-        }, [&](int i) { p[i] = fma(beta, p[i], r[i]); });
+        }, [&](int i) { p[i] = fma(beta, p[i], *R.at(i)); });
       } else {
         cg_rows4(row0, row1, true, [&](int i) {
           T rv[4];
-          ld4(r + i, rv);
+          ld4(R.at(i), rv);
           st4(p + i, rv);
-        }, [&](int i) { p[i] = r[i]; });
+        }, [&](int i) { p[i] = *R.at(i); });
       }
       if (!gs.gb.sync()) return;
       auto pg = [&](int c) { return p[c]; };
@@ -602,9 +671,9 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
         ld4(p + i, pv);
 #pragma unroll
         for (int u = 0; u < 4; u++) pap_t = fma(pv[u], av[u], pap_t);
-        st4(Ap + i, av);
+        st4(AP.at(i), av);
       }, [&](int i, T api) {
-        Ap[i] = api;
+        *AP.at(i) = api;
         pap_t = fma(p[i], api, pap_t);
       });
     }
@@ -624,23 +693,27 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
     T rrn_t = T(0);
     cg_rows4(row0, row1, xvec, [&](int i) {
       T xv[4], pv[4], av[4], rv[4];
-      ld4(x + i, xv);
+      T* const xi = X.at(i);
+      T* const ri = R.at(i);
+      ld4(xi, xv);
       ld4(p + i, pv);
-      ld4(Ap + i, av);
-      ld4(r + i, rv);
+      ld4(AP.at(i), av);
+      ld4(ri, rv);
 #pragma unroll
       for (int u = 0; u < 4; u++) {
         xv[u] = fma(alpha, pv[u], xv[u]);
         rv[u] = fma(-alpha, av[u], rv[u]);
         rrn_t = fma(rv[u], rv[u], rrn_t);
       }
-      st4(x + i, xv);
-      st4(r + i, rv);
+      st4(xi, xv);
+      st4(ri, rv);
     }, [&](int i) {
-      x[i] = fma(alpha, p[i], x[i]);
-      const T ri = fma(-alpha, Ap[i], r[i]);
-      r[i] = ri;
-      rrn_t = fma(ri, ri, rrn_t);
+      T* const xi = X.at(i);
+      *xi = fma(alpha, p[i], *xi);
+      T* const rp = R.at(i);
+      const T rn = fma(-alpha, *AP.at(i), *rp);
+      *rp = rn;
+      rrn_t = fma(rn, rn, rrn_t);
     });
     double rrn;
     if constexpr (FUSE) {
@@ -653,6 +726,10 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
     r1 = T(rrn);
     k++;
   }
+  // the resident rows back to global memory: x (the caller's solution) and r
+  // (read by a checkpoint)
+  X.store(row0, row1);
+  R.store(row0, row1);
   if (blockIdx.x == 0 && tid == 0) {
     *P.out_iter = k - 1;
     P.out_rr[0] = double(r1);
@@ -664,24 +741,29 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
 
 // ---------------------------------------------------------------------------
 // Mixed precision: FP32 Krylov iteration, FP64 solution and true residual.
+// Shared-memory residency as in cg_persistent: the FP32 r (unless the SpMV
+// gathers it), the FP32 increment x_s and Ap keep the CTA's rows on chip.
 template <int FMT, int FMT64>  // FMT64: the format of the FP64 matrix as given (CSR or DIA)
 __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant__ CgParams P) {
+  constexpr bool FUSE = FMT != 0 && FMT != 3;  // p formed where the SpMV gathers it (r gathered)
   const CgMat& A = P.A;      // FP32 iteration (values in val32)
   const CgMat& A64 = P.A64;  // FP64 true residual
   const double* __restrict__ val64 = static_cast<const double*>(A64.val);
   float* __restrict__ val32 = P.val32;
   const double* __restrict__ b = static_cast<const double*>(P.b);
   double* __restrict__ x = static_cast<double*>(P.x);
-  double* __restrict__ r64 = P.r64;
-  float* __restrict__ r = static_cast<float*>(P.r);
-  float* __restrict__ Ap = static_cast<float*>(P.Ap);
-  float* __restrict__ xs = P.xs;
+  float* __restrict__ r = static_cast<float*>(P.r);  // global r (gathered when FUSE)
   const int G = gridDim.x;
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
   const int2 sr = cta_slices<FMT>(A);
   GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G), P.ctl}};
   const int tid = threadIdx.x, nt = blockDim.x;
   const bool v4 = A.fmt != 0 && (A.n & 3) == 0 && aligned16(A.eci);  // val32 (workspace) is aligned
+  int off = 0;
+  // SELL: the SpMV writes rows of other CTAs (Ap): global
+  const RowVec<float> R = row_vec<float>(r, FUSE ? 0 : P.cap_r, row0, row1, off);
+  const RowVec<float> XS = row_vec<float>(P.xs, P.cap_x, row0, row1, off);
+  const RowVec<float> AP = row_vec<float>(static_cast<float*>(P.Ap), FMT == 3 ? 0 : P.cap_ap, row0, row1, off);
 
   // body(i, (A64 x)_i) for every row of this CTA: CSR by lane groups, else
   // one row per thread (rows split as for A: A64 has the same rows)
@@ -692,36 +774,53 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       CG_ROWS(i, { body(i, spmv_row<FMT64>(A64, val64, x, i)); })
     }
   };
-  // true residual in FP64
-  double rr = 0.0, bb = 0.0;
-  true_rows([&](int i, double ax) {
-    const double bi = b[i];
-    const double ri = bi - ax;
-    r64[i] = ri;
-    r[i] = float(ri);
-    xs[i] = 0.0f;
-    rr = fma(ri, ri, rr);
-    bb = fma(bi, bi, bb);
-  });
-  if (!gs.sum2(0, rr, bb)) return;
+  double rr, bb, maxrr, rr0;
+  int k, outer, since;
+  if (P.resume) {  // r, x_s and the last p restored by the host
+    R.load(row0, row1);
+    XS.load(row0, row1);
+    __syncthreads();
+    rr = P.rr0;
+    rr0 = P.rrp0;
+    bb = P.bb0;
+    maxrr = P.maxrr0;
+    k = P.k0 + 1;
+    outer = P.outer0;
+    since = P.since0;
+  } else {
+    // true residual in FP64
+    rr = 0.0;
+    bb = 0.0;
+    true_rows([&](int i, double ax) {
+      const double bi = b[i];
+      const double ri = bi - ax;
+      *R.at(i) = float(ri);
+      *XS.at(i) = 0.0f;
+      rr = fma(ri, ri, rr);
+      bb = fma(bi, bi, bb);
+    });
+    if (!gs.sum2(0, rr, bb)) return;
+    maxrr = rr;
+    rr0 = 0.0;
+    k = 1;
+    outer = 0;
+    since = 0;
+  }
   const double tol2 = (P.stop == PERKS_STOP_REL) ? P.tol * P.tol * bb : P.tol * P.tol;
-  double maxrr = rr, rr0 = 0.0;
-  int k = 1, outer = 0, since = 0;
   while (true) {
     if (!P.static_iter && rr < tol2) break;
     if (k > P.max_iter) break;
-    // p = r (first) or beta p_old + r, formed where it is gathered (the
-    // values its owner stores are the same fma)
+    // p = r (first) or beta p_old + r; iteration k writes P.p[k & 1]
     float* __restrict__ p = static_cast<float*>(P.p[k & 1]);
     float pap_t = 0.0f;
-    if constexpr (FMT == 0 || FMT == 3) {
+    if constexpr (!FUSE) {
       // CSR / SELL: p in its own pass (same values as the fused form), so
       // that the SpMV gathers one vector instead of two
       const float beta = k > 1 ? float(rr / rr0) : 0.0f;
       const float* __restrict__ po = static_cast<const float*>(P.p[(k + 1) & 1]);
       cg_rows4(row0, row1, true, [&](int i) {
         float pv[4], rv[4];
-        ld4(r + i, rv);
+        ld4(R.at(i), rv);
         if (k > 1) {
           ld4(po + i, pv);
 #pragma unroll
@@ -731,14 +830,15 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
           for (int u = 0; u < 4; u++) pv[u] = rv[u];
         }
         st4(p + i, pv);
-      }, [&](int i) { p[i] = k > 1 ? fmaf(beta, po[i], r[i]) : r[i]; });
+      }, [&](int i) { p[i] = k > 1 ? fmaf(beta, po[i], *R.at(i)) : *R.at(i); });
       if (!gs.gb.sync()) return;
       auto pgat = [&](int c) { return p[c]; };
       cg_rows_spmv<FMT, float>(A, val32, pgat, row0, row1, sr, [&](int) {}, [&](int i, float api) {
-        Ap[i] = api;
+        *AP.at(i) = api;
         pap_t = fmaf(p[i], api, pap_t);
       });
     } else if (k > 1) {
+      // formed where it is gathered (the values its owner stores are the same fma)
       const float beta = float(rr / rr0);
       const float* __restrict__ po = static_cast<const float*>(P.p[(k + 1) & 1]);
       auto pg = [&](int c) { return fmaf(beta, po[c], r[c]); };
@@ -753,11 +853,11 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
           pap_t = fmaf(pv[u], av[u], pap_t);
         }
         st4(p + i, pv);
-        st4(Ap + i, av);
+        st4(AP.at(i), av);
       }, [&](int i, float api) {
         const float pi = fmaf(beta, po[i], r[i]);
         p[i] = pi;
-        Ap[i] = api;
+        *AP.at(i) = api;
         pap_t = fmaf(pi, api, pap_t);
       });
     } else {
@@ -769,11 +869,11 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
 #pragma unroll
         for (int u = 0; u < 4; u++) pap_t = fmaf(rv[u], av[u], pap_t);
         st4(p + i, rv);
-        st4(Ap + i, av);
+        st4(AP.at(i), av);
       }, [&](int i, float api) {
         const float pi = r[i];
         p[i] = pi;
-        Ap[i] = api;
+        *AP.at(i) = api;
         pap_t = fmaf(pi, api, pap_t);
       });
     }
@@ -787,41 +887,48 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
     float rrn_t = 0.0f;
     cg_rows4(row0, row1, true, [&](int i) {
       float xv[4], pv[4], av[4], rv[4];
-      ld4(xs + i, xv);
+      float* const xi = XS.at(i);
+      float* const ri = R.at(i);
+      ld4(xi, xv);
       ld4(p + i, pv);
-      ld4(Ap + i, av);
-      ld4(r + i, rv);
+      ld4(AP.at(i), av);
+      ld4(ri, rv);
 #pragma unroll
       for (int u = 0; u < 4; u++) {
         xv[u] = fmaf(alpha, pv[u], xv[u]);
         rv[u] = fmaf(-alpha, av[u], rv[u]);
         rrn_t = fmaf(rv[u], rv[u], rrn_t);
       }
-      st4(xs + i, xv);
-      st4(r + i, rv);
+      st4(xi, xv);
+      st4(ri, rv);
     }, [&](int i) {
-      xs[i] = fmaf(alpha, p[i], xs[i]);
-      const float ri = fmaf(-alpha, Ap[i], r[i]);
-      r[i] = ri;
-      rrn_t = fmaf(ri, ri, rrn_t);
+      float* const xi = XS.at(i);
+      *xi = fmaf(alpha, p[i], *xi);
+      float* const rp = R.at(i);
+      const float rn = fmaf(-alpha, *AP.at(i), *rp);
+      *rp = rn;
+      rrn_t = fmaf(rn, rn, rrn_t);
     });
     double rrn;
     if (!gs.sum1f(3, rrn_t, rrn)) return;
     since++;
+    // the last allowed iteration folds x_s into x, unless a checkpoint takes
+    // the state (then x_s is saved with it and the resumed solve continues
+    // exactly as an uninterrupted one)
     const bool update = rrn < P.delta2 * maxrr || rrn < tol2 || (P.replace_every > 0 && since >= P.replace_every) ||
-                        k == P.max_iter;
+                        (k == P.max_iter && !P.keep_state);
     if (update) {
       // x += xs in FP64; true residual with the FP64 matrix
       CG_ROWS(i, {
-        x[i] += double(xs[i]);
-        xs[i] = 0.0f;
+        float* const xi = XS.at(i);
+        x[i] += double(*xi);
+        *xi = 0.0f;
       })
       if (!gs.gb.sync()) return;
       double rt = 0.0;
       true_rows([&](int i, double ax) {
         const double ri = b[i] - ax;
-        r64[i] = ri;
-        r[i] = float(ri);
+        *R.at(i) = float(ri);
         rt = fma(ri, ri, rt);
       });
       if (!gs.sum1(0, rt)) return;
@@ -834,9 +941,16 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
     rr = rrn;
     k++;
   }
+  // resident rows back to global memory (read by a checkpoint)
+  R.store(row0, row1);
+  XS.store(row0, row1);
   if (blockIdx.x == 0 && tid == 0) {
     *P.out_iter = k - 1;
-    *P.out_rr = rr;
+    P.out_rr[0] = rr;
+    P.out_rr[1] = rr0;
+    P.out_rr[2] = bb;
+    P.out_rr[3] = maxrr;
+    P.out_rr[4] = double(since);
     *P.out_outer = outer;
   }
 }
@@ -1154,8 +1268,9 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
     return fail(PERKS_ERR_UNSUPPORTED, "mixed precision runs in the persistent kernel only");
   perks_cg_state* ck = o->checkpoint;
   if (ck) {
-    if (o->dtype == PERKS_MIXED) return fail(PERKS_ERR_UNSUPPORTED, "no checkpoint for mixed precision");
     if (!ck->d_r || !ck->d_p || ck->k < 0) return fail(PERKS_ERR_INVALID_ARG, "bad checkpoint");
+    if (o->dtype == PERKS_MIXED && !ck->d_xs)
+      return fail(PERKS_ERR_INVALID_ARG, "a mixed-precision checkpoint needs d_xs");
     if (ck->k > 0 && ck->kernel != o->kernel)
       return fail(PERKS_ERR_INVALID_ARG, "checkpoint was written by the other kernel kind");
     // d_r and d_p hold n elements of the writer's working type: a different
@@ -1176,11 +1291,10 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   int st = PERKS_OK;
   const int ctas = o->ctas > 0 ? std::min(o->ctas, dev->sms) : dev->sms;
   const size_t vbytes = (size_t(n) * ws + 255) & ~size_t(255);
-  const size_t v64 = (size_t(n) * 8 + 255) & ~size_t(255);
   const size_t nval = A.fmt == 0 ? size_t(A.nnz) : size_t(A.ndiag) * n;
   constexpr size_t kTail = 80 * 1024;   // partial sums (4 slots x 2 x 1024 CTAs) + scalars
   size_t need = 4 * vbytes + kTail;     // r, p (two buffers), Ap + tail
-  if (o->dtype == PERKS_MIXED) need += v64 + vbytes + ((nval * 4 + 255) & ~size_t(255));
+  if (o->dtype == PERKS_MIXED) need += vbytes + ((nval * 4 + 255) & ~size_t(255));  // x_s, FP32 values
   unsigned char* w = static_cast<unsigned char*>(workspace(kWsCgVec, need, &st));
   if (!w) return st;
   SyncWords sw;
@@ -1198,9 +1312,8 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   double* scal = P.part + 8 * 1024;                    // device scalars / results (32 doubles)
   unsigned char* more = tail + kTail;
   if (o->dtype == PERKS_MIXED) {
-    P.r64 = reinterpret_cast<double*>(more);
-    P.xs = reinterpret_cast<float*>(more + v64);
-    P.val32 = reinterpret_cast<float*>(more + v64 + vbytes);
+    P.xs = reinterpret_cast<float*>(more);
+    P.val32 = reinterpret_cast<float*>(more + vbytes);
   }
   P.tol = o->tol;
   P.stop = o->stop;
@@ -1210,13 +1323,17 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   P.delta2 = 0.1 * 0.1;
   P.out_iter = reinterpret_cast<int*>(scal + 16);
   P.out_outer = reinterpret_cast<int*>(scal + 17);
-  P.out_rr = scal + 18;  // [18..20]
+  P.out_rr = scal + 18;  // [18..22]
+  P.keep_state = ck != nullptr;
   if (resume) {
     P.resume = 1;
     P.k0 = ck->k;
     P.rr0 = ck->rr;
     P.rrp0 = ck->rr_prev;
     P.bb0 = ck->bb;
+    P.maxrr0 = ck->maxrr;
+    P.outer0 = ck->outer;
+    P.since0 = ck->since;
   }
   P.bar = sw.bar;
   P.status = sw.status;
@@ -1375,11 +1492,13 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   // (DIA, ELL) alternate two buffers (iteration k writes P.p[k & 1]); the
   // others keep p in P.p[0]
   auto p_of = [&](int k) {
-    return (f32 && o->kernel == PERKS_KERNEL_PERSISTENT && P.A.fmt != 0 && P.A.fmt != 3) ? P.p[k & 1] : P.p[0];
+    const bool fused32 = f32 && o->kernel == PERKS_KERNEL_PERSISTENT && P.A.fmt != 0 && P.A.fmt != 3;
+    return (fused32 || mixed) ? P.p[k & 1] : P.p[0];
   };
   if (resume) {
     PERKS_CUDA(cudaMemcpyAsync(P.r, ck->d_r, size_t(n) * ws, cudaMemcpyDeviceToDevice, s));
     PERKS_CUDA(cudaMemcpyAsync(p_of(ck->k), ck->d_p, size_t(n) * ws, cudaMemcpyDeviceToDevice, s));
+    if (mixed) PERKS_CUDA(cudaMemcpyAsync(P.xs, ck->d_xs, size_t(n) * 4, cudaMemcpyDeviceToDevice, s));
   }
   int launches = 0;
   if (o->kernel == PERKS_KERNEL_PERSISTENT) {
@@ -1394,11 +1513,41 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
                  : f == 2 ? (const void*)cg_persistent<float, 2> : (const void*)cg_persistent<float, 3>)
               : (f == 0 ? (const void*)cg_persistent<double, 0> : f == 1 ? (const void*)cg_persistent<double, 1>
                  : f == 2 ? (const void*)cg_persistent<double, 2> : (const void*)cg_persistent<double, 3>);
+    // Shared memory for the vectors that only their owning CTA touches, in
+    // order of accesses saved per iteration: r (3, unless the SpMV gathers
+    // it or, SELL, writes rows of other CTAs), x or the mixed increment x_s
+    // (2), Ap (2, not SELL). Each takes its CTA's rows up to what is left of
+    // the budget; rows past a cap stream through global memory. The budget
+    // is taken from the L1 cache (one 256 KB store per SM), on which the
+    // SpMV gathers depend: measured on GB300, a full carve-out (~220 KB)
+    // made every solve slower (2D Laplacian 2048^2 FP64 130 vs 107 us per
+    // iteration), so the default keeps nothing resident.
+    cudaFuncAttributes fa{};
+    PERKS_CUDA(cudaFuncGetAttributes(&fa, kern));
+    const bool gathered_r = ((f32 || mixed) && (f == 1 || f == 2)) || f == 3;
+    const size_t es = ws;  // FP64 / FP32; mixed: the FP32 r, x_s, Ap
+    const long long most = (long long)dev->smem_optin - (long long)fa.sharedSizeBytes - 256;
+    long long budget = o->cache_vectors > 0 ? std::min<long long>(most, 1024ll * o->cache_vectors) : 0;
+    // rows of the CTA with the most: DIA/ELL split evenly; CSR (merge path)
+    // and SELL (whole 1024-row windows) vary around n / ctas
+    const long long even = (n + ctas - 1) / ctas;
+    const long long span = (f == 1 || f == 2) ? even + 4 : std::min<long long>(n + 4, even + even / 4 + 1028);
+    auto take = [&](bool allowed) {
+      if (!allowed || budget <= 0) return 0;
+      const long long rows = std::min<long long>((budget / (long long)es) & ~3ll, (span + 3) & ~3ll);
+      budget -= rows * (long long)es;
+      return int(rows);
+    };
+    P.cap_r = take(!gathered_r);
+    P.cap_x = take(true);
+    P.cap_ap = take(f != 3);
+    const size_t dsmem = size_t(P.cap_r + P.cap_x + P.cap_ap) * es;
+    PERKS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dsmem)));
     int per_sm = 0;
-    PERKS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCgThreads, 0));
+    PERKS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCgThreads, dsmem));
     if (per_sm < 1) return fail(PERKS_ERR_LAUNCH, "CG kernel does not fit on an SM");
     void* args[] = {&P};
-    cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(ctas), dim3(kCgThreads), args, 0, s);
+    cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(ctas), dim3(kCgThreads), args, dsmem, s);
     if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchCooperativeKernel(cg)");
     launches = 1;
   } else {
@@ -1461,13 +1610,15 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   PERKS_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, s));
   PERKS_CUDA(cudaStreamSynchronize(s));
   int iters = 0, outer = 0;
-  double rr = 0.0, rr_prev = 0.0, bbs = 0.0;
+  double rr = 0.0, rr_prev = 0.0, bbs = 0.0, maxrr = 0.0, since = 0.0;
   if (o->kernel == PERKS_KERNEL_PERSISTENT) {
     std::memcpy(&iters, &hs[16], sizeof(int));
     std::memcpy(&outer, &hs[17], sizeof(int));
     rr = hs[18];
     rr_prev = hs[19];
     bbs = hs[20];
+    maxrr = hs[21];
+    since = hs[22];
   } else {
     iters = int(hs[5]);
     rr = hs[0];
@@ -1477,9 +1628,13 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   if (ck) {  // state for a later resume
     PERKS_CUDA(cudaMemcpyAsync(ck->d_r, P.r, size_t(n) * ws, cudaMemcpyDeviceToDevice, s));
     PERKS_CUDA(cudaMemcpyAsync(ck->d_p, p_of(iters), size_t(n) * ws, cudaMemcpyDeviceToDevice, s));
+    if (mixed) PERKS_CUDA(cudaMemcpyAsync(ck->d_xs, P.xs, size_t(n) * 4, cudaMemcpyDeviceToDevice, s));
     ck->rr = rr;
     ck->rr_prev = rr_prev;
     ck->bb = bbs;
+    ck->maxrr = maxrr;
+    ck->outer = outer;
+    ck->since = int(since);
     ck->k = iters;
     ck->kernel = o->kernel;
     ck->dtype = o->dtype;
@@ -1491,10 +1646,10 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   const bool val_f32 = f32;
   if (val_f32) cg_true_residual<float><<<tg, 512, 0, s>>>(A, b, x, tpart);
   else cg_true_residual<double><<<tg, 512, 0, s>>>(A, b, x, tpart);
-  sum_partials<<<1, 1024, 0, s>>>(tpart, tg, scal + 22);
+  sum_partials<<<1, 1024, 0, s>>>(tpart, tg, scal + 28);
   count_launch(2);
   double tr[2];
-  PERKS_CUDA(cudaMemcpyAsync(tr, scal + 22, sizeof(tr), cudaMemcpyDeviceToHost, s));
+  PERKS_CUDA(cudaMemcpyAsync(tr, scal + 28, sizeof(tr), cudaMemcpyDeviceToHost, s));
   PERKS_CUDA(cudaStreamSynchronize(s));
   if (res) {
     res->iterations = iters;
@@ -1531,6 +1686,7 @@ void perks_cg_default_opts(perks_cg_opts* o) {
   o->ctas = 0;
   o->stream = nullptr;
   o->checkpoint = nullptr;
+  o->cache_vectors = -1;
 }
 
 int perks_cg_csr(int n, int nnz, const int* rp, const int* ci, const void* val, const void* b, void* x,

@@ -135,33 +135,37 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Vector loads/stores of a lane's V elements (NV 16-byte vectors).
-template <int NV>
+// Vector loads/stores of a lane's V elements (NV 16-byte vectors), vector k
+// at src + k * S elements: S = 16 bytes for a lane's contiguous columns in
+// the field; S = 32 x 16 bytes for the vector-major shared-memory rows, where
+// vector k of lane l sits at (32 k + l) x 16 bytes, so that each warp-wide
+// vector access is one contiguous 512-byte run (no bank conflicts).
+template <int NV, int S = 4>
 __device__ __forceinline__ void load_lane(const float* src, float (&o)[4 * NV]) {
 #pragma unroll
   for (int k = 0; k < NV; k++) {
-    const float4 v = reinterpret_cast<const float4*>(src)[k];
+    const float4 v = *reinterpret_cast<const float4*>(src + k * S);
     o[4 * k] = v.x; o[4 * k + 1] = v.y; o[4 * k + 2] = v.z; o[4 * k + 3] = v.w;
   }
 }
-template <int NV>
+template <int NV, int S = 2>
 __device__ __forceinline__ void load_lane(const double* src, double (&o)[2 * NV]) {
 #pragma unroll
   for (int k = 0; k < NV; k++) {
-    const double2 v = reinterpret_cast<const double2*>(src)[k];
+    const double2 v = *reinterpret_cast<const double2*>(src + k * S);
     o[2 * k] = v.x; o[2 * k + 1] = v.y;
   }
 }
-template <int NV>
+template <int NV, int S = 4>
 __device__ __forceinline__ void store_lane(float* dst, const float (&o)[4 * NV]) {
 #pragma unroll
   for (int k = 0; k < NV; k++)
-    reinterpret_cast<float4*>(dst)[k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+    *reinterpret_cast<float4*>(dst + k * S) = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
 }
-template <int NV>
+template <int NV, int S = 2>
 __device__ __forceinline__ void store_lane(double* dst, const double (&o)[2 * NV]) {
 #pragma unroll
-  for (int k = 0; k < NV; k++) reinterpret_cast<double2*>(dst)[k] = make_double2(o[2 * k], o[2 * k + 1]);
+  for (int k = 0; k < NV; k++) *reinterpret_cast<double2*>(dst + k * S) = make_double2(o[2 * k], o[2 * k + 1]);
 }
 
 // A window row in registers: V values of this lane and one edge value.
@@ -222,7 +226,8 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
   const int edge_col = lane < H ? max(x0 - 1 - lane, 0) : min(x0 + SW + (lane - H), wx - 1);
   const int edge_chunk = (edge_col / V16) * V16;
   const int edge_sub = edge_col - edge_chunk;
-  T* const my_ring_v = ring + lane * V;                   // this lane's columns in a slot
+  constexpr int VS = 32 * V16;                           // vector stride of the shared-memory rows
+  T* const my_ring_v = ring + lane * V16;                 // this lane's first vector in a slot (vector-major)
   T* const my_ring_e = ring + SW + min(lane, 2 * H - 1) * V16;  // this edge lane's chunk in a slot
   // Shuffle sources and selectors of the horizontal window (row independent).
   int src_l[H], src_r[H];
@@ -241,7 +246,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
   const F2 one2(p.one);
   bool ok = true;
 
-  auto res_ptr = [&](int r) -> T* { return res + (size_t(r - rres0) * NW + wid) * SW + lane * V; };
+  auto res_ptr = [&](int r) -> T* { return res + (size_t(r - rres0) * NW + wid) * SW + lane * V16; };
   auto is_res = [&](int r) { return r >= rres0 && r < rres0 + C; };
 
   if (C > 0) {
@@ -249,7 +254,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
     for (int k = 0; k < C; k++) {
       T v[V];
       load_lane<NV>(fin + size_t(rres0 + k) * pitch + xl, v);
-      store_lane<NV>(res_ptr(rres0 + k), v);
+      store_lane<NV, VS>(res_ptr(rres0 + k), v);
     }
   }
 
@@ -274,7 +279,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
           if (!is_res(r)) {
             const uint64_t pl = (alt && interior(r)) ? pol_first : pol;
 #pragma unroll
-            for (int k = 0; k < NV; k++) cp_async16(my_ring_v + size_t(sf) * SLOT + k * V16, src + xl + k * V16, pl);
+            for (int k = 0; k < NV; k++) cp_async16(my_ring_v + size_t(sf) * SLOT + k * VS, src + xl + k * V16, pl);
           }
           if (edge_lane) cp_async16(slot + SW + lane * V16, src + edge_chunk, pol);
         }
@@ -286,7 +291,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
         RowT out;
         const int r = row_of(q);
         const bool rr = is_res(r);
-        load_lane<NV>(rr ? res_ptr(r) : my_ring_v + size_t(sl) * SLOT, out.v);
+        load_lane<NV, VS>(rr ? res_ptr(r) : my_ring_v + size_t(sl) * SLOT, out.v);
         out.e = edge_lane ? my_ring_e[size_t(sl) * SLOT + edge_sub] : T(0);
         if (ghost_strip) {
           // elements beyond the last column take that column's value
@@ -394,7 +399,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
         }
         T* dst = fout + size_t(y) * pitch + xl;
         if (is_res(y)) {
-          store_lane<NV>(res_ptr(y), o);
+          store_lane<NV, VS>(res_ptr(y), o);
           if (lane * V < H || (lane + 1) * V > SW - H) store_lane<NV>(dst, o);
         } else {
           store_lane<NV>(dst, o);
@@ -456,7 +461,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
     T* fnew = static_cast<T*>(p.f[(p.t0 + p.steps) & 1]);
     for (int k = 0; k < C; k++) {
       T v[V];
-      load_lane<NV>(res_ptr(rres0 + k), v);
+      load_lane<NV, VS>(res_ptr(rres0 + k), v);
       store_lane<NV>(fnew + size_t(rres0 + k) * pitch + xl, v);
     }
   }

@@ -38,7 +38,9 @@ def _build(cuda, torch, seed=7):
         stencils.append((len(jobs), shape, f, steps, o))
         jobs.append(stencil_job(a, o, shape, steps))
     for k, (mat, dt, tol) in enumerate([("lap2d", np.float64, 1e-10), ("lap3d", np.float64, 1e-10),
-                                         ("lap2d", np.float32, 1e-5), ("spd", np.float64, 1e-10)]):
+                                         ("lap2d", np.float32, 1e-5), ("spd", np.float64, 1e-10),
+                                         ("lap2d", "mixed", 1e-10), ("spd", "mixed", 1e-10),
+                                         ("lap3d", "mixed", 1e-10)]):
         rp, ci, v = {"lap2d": lambda: M.laplacian_2d(40), "lap3d": lambda: M.laplacian_3d(14),
                      "spd": lambda: M.random_spd(3000, 2)}[mat]()
         rp, ci, v = M.shifted(rp, ci, v, 0.1 * (k + 1))
@@ -47,7 +49,8 @@ def _build(cuda, torch, seed=7):
         dev = lambda a, t: torch.from_numpy(np.ascontiguousarray(a)).to(cuda, t)
         x = torch.empty(len(b), dtype=tt, device=cuda)
         cgs.append((len(jobs), rp, ci, v, b, tol, dt, x))
-        jobs.append(cg_job(dev(rp, torch.int32), dev(ci, torch.int32), dev(v, tt), dev(b, tt), x, tol=tol, max_iter=5000))
+        jobs.append(cg_job(dev(rp, torch.int32), dev(ci, torch.int32), dev(v, tt), dev(b, tt), x, tol=tol, max_iter=5000,
+                           mixed=dt == "mixed"))
     return jobs, stencils, cgs
 
 
@@ -73,10 +76,13 @@ def test_batch_matches_oracle(native, cuda, oracle, threads, ctas):
                 assert res[j]["rel_res"] <= tol
                 xs = x.cpu().numpy().astype(np.float64)
                 r = b - oracle.spmv_csr(rp, ci, np.asarray(v, np.float64), xs)
-                assert np.linalg.norm(r) / np.linalg.norm(b) <= (tol * 1.05 if dt == np.float64 else 1e-4)
-                if dt == np.float64:
+                assert np.linalg.norm(r) / np.linalg.norm(b) <= (1e-4 if dt == np.float32 else tol * 1.05)
+                if dt != np.float32:
                     _, it, _, _ = oracle.cg(rp, ci, v, b, max_iter=5000, stop=1, tol=tol)
-                    assert it_close(res[j]["iterations"], it), (res[j], it)
+                    if dt == "mixed":  # FP32 inner iterations: more of them, the FP64 accuracy
+                        assert res[j]["iterations"] <= 2 * it + 50, (res[j], it)
+                    else:
+                        assert it_close(res[j]["iterations"], it), (res[j], it)
 
 
 def test_batch_rejects_bad_jobs(native, cuda):

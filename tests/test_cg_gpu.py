@@ -182,7 +182,10 @@ def test_cg_csr_layouts(native, cuda, oracle, layout, expect, dtype):
         xo, _, _, _ = oracle.cg(rp, ci, v32, b32, max_iter=8, static_iter=True)
         x, res = native.cg_csr(rp, ci, v32, b32, dtype="fp32", max_iter=8, static_iter=True, device=cuda)
         assert res["layout"] == expect
-        assert np.allclose(x.cpu().numpy(), xo, rtol=2e-4, atol=1e-5)
+        # normwise: the arrow's dense row sums 20000 FP32 terms with
+        # cancellation, in another order than the sequential oracle
+        xg = x.cpu().numpy().astype(np.float64)
+        assert np.linalg.norm(xg - xo) <= 1e-4 * np.linalg.norm(xo)
         return
     x, res = native.cg_csr(rp, ci, v, b, dtype=dtype, tol=1e-10, device=cuda)
     assert res["layout"] == expect, res

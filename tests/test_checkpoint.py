@@ -31,8 +31,10 @@ def _solve(native, cuda, prob, dtype, x0=None, **kw):
 
 @pytest.mark.parametrize("fmt", ["csr", "dia"])
 @pytest.mark.parametrize("kernel", ["persistent", "per_step"])
-@pytest.mark.parametrize("dtype", ["fp64", "fp32"])
+@pytest.mark.parametrize("dtype", ["fp64", "fp32", "mixed"])
 def test_cg_resume_static_bit_exact(native, cuda, dtype, kernel, fmt):
+    if dtype == "mixed" and kernel == "per_step":
+        pytest.skip("mixed precision runs in the persistent kernel only")
     prob = _problem(fmt)
     full = native.CgCheckpoint()
     x_full, res = _solve(native, cuda, prob, dtype, max_iter=60, static_iter=True, kernel=kernel, checkpoint=full)
@@ -45,16 +47,20 @@ def test_cg_resume_static_bit_exact(native, cuda, dtype, kernel, fmt):
     x2, r2 = _solve(native, cuda, prob, dtype, x0=x1, max_iter=60, static_iter=True, kernel=kernel,
                     checkpoint=ck2)
     assert r2["iterations"] == 60 and ck2.k == 60
-    for a, b in ((x2, x_full), (ck2.r, full.r), (ck2.p, full.p)):
+    pairs = [(x2, x_full), (ck2.r, full.r), (ck2.p, full.p)] + ([(ck2.xs, full.xs)] if dtype == "mixed" else [])
+    for a, b in pairs:
         assert bits_equal(a.cpu().numpy(), b.cpu().numpy())
     assert r2["rr"] == res["rr"] and ck2.state.rr_prev == full.state.rr_prev
+    assert ck2.state.outer == full.state.outer and ck2.state.maxrr == full.state.maxrr
 
 
 @pytest.mark.parametrize("kernel", ["persistent", "per_step"])
-@pytest.mark.parametrize("dtype", ["fp64", "fp32"])
+@pytest.mark.parametrize("dtype", ["fp64", "fp32", "mixed"])
 def test_cg_resume_after_cap(native, cuda, dtype, kernel):
+    if dtype == "mixed" and kernel == "per_step":
+        pytest.skip("mixed precision runs in the persistent kernel only")
     prob = _problem("csr")
-    tol = 1e-10 if dtype == "fp64" else 1e-4
+    tol = 1e-4 if dtype == "fp32" else 1e-10
     x_full, res = _solve(native, cuda, prob, dtype, tol=tol, kernel=kernel)
     K = res["iterations"]
     ck = native.CgCheckpoint()
@@ -100,10 +106,10 @@ def test_cg_checkpoint_rejects_misuse(native, cuda):
     _solve(native, cuda, prob, "fp64", max_iter=5, static_iter=True, kernel="persistent", checkpoint=ck)
     with pytest.raises(native.PerksError):  # written by the persistent kernel
         _solve(native, cuda, prob, "fp64", max_iter=9, static_iter=True, kernel="per_step", checkpoint=ck)
-    with pytest.raises(native.PerksError):  # no mixed-precision state
-        _solve(native, cuda, prob, "mixed", checkpoint=native.CgCheckpoint())
     with pytest.raises(ValueError):  # FP64 state, FP32 solve
         _solve(native, cuda, prob, "fp32", checkpoint=ck)
+    with pytest.raises(ValueError):  # FP64 state, mixed solve (FP32 r and p)
+        _solve(native, cuda, prob, "mixed", checkpoint=ck)
 
 
 @pytest.mark.parametrize("shape,dt", [("2ds9pt", np.float32), ("2d9pt", np.float64), ("3d7pt", np.float32),
