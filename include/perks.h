@@ -235,6 +235,10 @@ typedef struct {
                          0 = none, -1 = the library's default (none: the shared memory is taken
                          from the L1 cache that the SpMV gathers use, and on GB300 that cost more
                          than it saved) */
+  int cluster;        /* persistent kernel: CTAs per thread-block cluster (1 = none, default; 2, 4,
+                         8, 16): the CTAs of a cluster combine their dot-product partials over
+                         distributed shared memory and only one CTA per cluster takes part in the
+                         grid barrier; the grid is then as many whole clusters as fit at once */
 } perks_cg_opts;
 
 typedef struct {
@@ -246,6 +250,7 @@ typedef struct {
   int launches;
   int layout;            /* matrix layout the iteration ran on: 0 CSR as given (lane groups per row),
                             1 DIA, 2 ELL, 3 SELL (copies made at the start of the solve) */
+  int ctas;              /* CTAs of the persistent launch */
 } perks_cg_result;
 
 PERKS_API void perks_cg_default_opts(perks_cg_opts* opts);

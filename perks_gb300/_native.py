@@ -54,12 +54,13 @@ class CgState(ctypes.Structure):
 class CgOpts(ctypes.Structure):
     _fields_ = [("dtype", c_int), ("stop", c_int), ("tol", c_double), ("max_iter", c_int),
                 ("static_iter", c_int), ("kernel", c_int), ("replace_every", c_int), ("ctas", c_int),
-                ("stream", c_void_p), ("checkpoint", ctypes.POINTER(CgState)), ("cache_vectors", c_int)]
+                ("stream", c_void_p), ("checkpoint", ctypes.POINTER(CgState)), ("cache_vectors", c_int),
+                ("cluster", c_int)]
 
 
 class CgResult(ctypes.Structure):
     _fields_ = [("iterations", c_int), ("outer", c_int), ("rr", c_double), ("true_rel_res", c_double),
-                ("ms", c_double), ("launches", c_int), ("layout", c_int)]
+                ("ms", c_double), ("launches", c_int), ("layout", c_int), ("ctas", c_int)]
 
 
 class Job(ctypes.Structure):

@@ -86,7 +86,7 @@ class CgCheckpoint:
 
 
 def _opts(dtype="fp64", stop="rel", tol=1e-10, max_iter=100000, static_iter=False, kernel="persistent",
-          replace_every=0, ctas=0, stream=None, cache_vectors=-1):
+          replace_every=0, ctas=0, stream=None, cache_vectors=-1, cluster=1):
     o = N.CgOpts()
     N.lib().perks_cg_default_opts(ctypes.byref(o))
     o.dtype = _DT[dtype]
@@ -99,6 +99,7 @@ def _opts(dtype="fp64", stop="rel", tol=1e-10, max_iter=100000, static_iter=Fals
     o.ctas = int(ctas)
     o.stream = stream
     o.cache_vectors = int(cache_vectors)
+    o.cluster = int(cluster)
     return o
 
 

@@ -98,6 +98,7 @@ struct CgParams {
   // rows per CTA kept in shared memory for the whole solve (multiples of 4;
   // 0 = streamed): r (or, mixed, its FP32 r), x (mixed: x_s), Ap
   int cap_r, cap_x, cap_ap;
+  int cluster;            // CTAs per thread-block cluster of the launch (1 = no cluster combine)
   // resume from a checkpoint: r and p already in place, scalars here
   int resume, k0;         // k0 = iterations completed before this launch
   double rr0, rrp0, bb0;
@@ -269,14 +270,101 @@ __device__ __forceinline__ void block_sum_t0(double (&v)[NV]) {
   }
 }
 
+constexpr int kMaxCluster = 16;
+
 // Grid-wide deterministic sum: every CTA stores its partials, one barrier,
 // then every CTA adds all partials in the same order.
+// With thread-block clusters (cl > 1, the launch's cluster size) the CTAs of
+// a cluster first combine their partials in the leader CTA's shared memory
+// over DSMEM (fixed rank order); only the leaders store partials and arrive
+// at the grid barrier (gb.nblocks = clusters), the leader adds the clusters'
+// partials in cluster order and hands the total back to its CTAs over DSMEM.
+// Every CTA of a cluster passes the same cluster barriers in the same order
+// (all decisions below depend only on values the whole cluster shares), so
+// no CTA waits on a cluster barrier that a peer skips; a failed wait ends the
+// kernel in every CTA after one more cluster barrier, so that no CTA leaves
+// while a peer still reads its shared memory.
 struct GridSum {
   double* part;  // [slot][2][gridDim]
   GridBarrier gb;
+  int cl = 1;
+  // every CTA of the cluster: the leader's flag, `ok`, after the grid barrier
+  __device__ bool cluster_barrier() {
+    __shared__ unsigned cl_ok;
+    gb.epoch++;
+    if (threadIdx.x == 0) __threadfence();  // this CTA's global writes, before the leader arrives
+    cluster_sync_all();
+    if (cluster_ctarank() == 0 && threadIdx.x < 32) {
+      unsigned ok = 0;
+      if (threadIdx.x == 0) ok = gb.arrive_wait(int(cluster_index_x())) ? 1u : 0u;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (threadIdx.x == 0) cl_ok = ok;
+    }
+    cluster_sync_all();
+    __shared__ unsigned my_ok;
+    if (threadIdx.x == 0) my_ok = dsmem_ld_u32(dsmem_addr(&cl_ok, 0));
+    cluster_sync_all();  // the leader's cl_ok is read before it may change or the leader may leave
+    return my_ok != 0;
+  }
+  __device__ bool bar() { return cl > 1 ? cluster_barrier() : gb.sync(); }
+  template <int NV>
+  __device__ bool sum_cluster(int slot, double (&v)[NV]) {
+    __shared__ double cl_part[kMaxCluster][NV];
+    __shared__ double cl_tot[NV];
+    __shared__ unsigned cl_ok;
+    const unsigned rank = cluster_ctarank();
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k < NV; k++) dsmem_st_f64(dsmem_addr(&cl_part[rank][k], 0), v[k]);
+      __threadfence();  // this CTA's global writes, before the leader arrives
+    }
+    gb.epoch++;
+    cluster_sync_all();
+    if (rank == 0 && threadIdx.x < 32) {
+      const int ncl = int(cluster_count_x());
+      double* ps = part + size_t(slot) * 2 * gridDim.x;
+      unsigned ok = 0;
+      if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+          double c = 0.0;
+          for (int r = 0; r < cl; r++) c += cl_part[r][k];
+          ps[k * ncl + int(cluster_index_x())] = c;
+        }
+        ok = gb.arrive_wait(int(cluster_index_x())) ? 1u : 0u;
+      }
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (ok) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+          double acc = 0.0;
+#pragma unroll 8
+          for (int i = threadIdx.x; i < ncl; i += 32) acc += __ldcg(ps + k * ncl + i);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+          if (threadIdx.x == 0) cl_tot[k] = acc;
+        }
+      }
+      if (threadIdx.x == 0) cl_ok = ok;
+    }
+    cluster_sync_all();
+    __shared__ double rs[NV];
+    __shared__ unsigned my_ok;
+    if (threadIdx.x == 0) {
+      my_ok = dsmem_ld_u32(dsmem_addr(&cl_ok, 0));
+#pragma unroll
+      for (int k = 0; k < NV; k++) rs[k] = dsmem_ld_f64(dsmem_addr(&cl_tot[k], 0));
+    }
+    cluster_sync_all();  // the leader's results are read before they may change or the leader may leave
+    if (my_ok == 0) return false;
+#pragma unroll
+    for (int k = 0; k < NV; k++) v[k] = rs[k];
+    return true;
+  }
   template <int NV, bool WARP_DONE = false>
   __device__ bool sum(int slot, double (&v)[NV]) {
     block_sum_t0<NV, WARP_DONE>(v);
+    if (cl > 1) return sum_cluster<NV>(slot, v);
     const int G = gridDim.x;
     double* ps = part + size_t(slot) * 2 * G;
     if (threadIdx.x == 0)
@@ -500,18 +588,21 @@ __device__ __forceinline__ void spmv4(const CgMat& A, const MV* __restrict__ val
   }
 }
 
-// A vector of which this CTA reads and writes only its own rows (never
-// gathered by another CTA): rows [base, cut) live in shared memory for the
-// whole solve, the rest in global memory (PERKS: the CTA's share of the
-// domain stays on chip across iterations and only the remainder streams).
-// base = row0 rounded down to 4 and cut - base is a multiple of 4, so a
-// four-row group is entirely on one side and 16-byte aligned there.
+// A vector of which this CTA keeps rows [base, cut) in shared memory for the
+// whole solve, the rest (and every row of other CTAs) in global memory
+// (PERKS: the CTA's share of the domain stays on chip across iterations and
+// only the remainder streams). base = row0 rounded down to 4 and cut - base is
+// a multiple of 4, so a four-row group is entirely on one side and 16-byte
+// aligned there. at() checks both ends: a SELL SpMV writes rows of other
+// CTAs, below base as well as above cut.
 template <class T>
 struct RowVec {
   T* g;
   T* s;
   int base, cut;
-  __device__ __forceinline__ T* at(int i) const { return i < cut ? s + (i - base) : g + i; }
+  __device__ __forceinline__ T* at(int i) const {
+    return unsigned(i - base) < unsigned(cut - base) ? s + (i - base) : g + i;
+  }
   // global -> shared (rows [lo, hi) of the CTA), or back
   __device__ __forceinline__ void load(int lo, int hi) const {
     for (int i = lo + threadIdx.x; i < min(hi, cut); i += blockDim.x) s[i - base] = g[i];
@@ -549,7 +640,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
   const int G = gridDim.x;
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
   const int2 sr = cta_slices<FMT>(A);
-  GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G), P.ctl}};
+  GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(P.cluster > 1 ? G / P.cluster : G), P.ctl}, P.cluster};
   const int tid = threadIdx.x, nt = blockDim.x;
   const bool xvec = aligned16(P.x);  // the caller's solution vector
   const bool v4 = A.fmt != 0 && (A.n & 3) == 0 && aligned16(val) && aligned16(A.eci);  // DIA/ELL columns 16-byte aligned
@@ -663,7 +754,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
           st4(p + i, rv);
         }, [&](int i) { p[i] = *R.at(i); });
       }
-      if (!gs.gb.sync()) return;
+      if (!gs.bar()) return;
       auto pg = [&](int c) { return p[c]; };
       cg_rows_spmv<FMT, T>(A, val, pg, row0, row1, sr, [&](int i) {
         T av[4], pv[4];
@@ -756,7 +847,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
   const int G = gridDim.x;
   const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
   const int2 sr = cta_slices<FMT>(A);
-  GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(G), P.ctl}};
+  GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(P.cluster > 1 ? G / P.cluster : G), P.ctl}, P.cluster};
   const int tid = threadIdx.x, nt = blockDim.x;
   const bool v4 = A.fmt != 0 && (A.n & 3) == 0 && aligned16(A.eci);  // val32 (workspace) is aligned
   int off = 0;
@@ -831,7 +922,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
         }
         st4(p + i, pv);
       }, [&](int i) { p[i] = k > 1 ? fmaf(beta, po[i], *R.at(i)) : *R.at(i); });
-      if (!gs.gb.sync()) return;
+      if (!gs.bar()) return;
       auto pgat = [&](int c) { return p[c]; };
       cg_rows_spmv<FMT, float>(A, val32, pgat, row0, row1, sr, [&](int) {}, [&](int i, float api) {
         *AP.at(i) = api;
@@ -924,7 +1015,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
         x[i] += double(*xi);
         *xi = 0.0f;
       })
-      if (!gs.gb.sync()) return;
+      if (!gs.bar()) return;
       double rt = 0.0;
       true_rows([&](int i, double ax) {
         const double ri = b[i] - ax;
@@ -1290,6 +1381,12 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   const size_t ws = f32 || o->dtype == PERKS_MIXED ? 4 : 8;  // working precision bytes
   int st = PERKS_OK;
   const int ctas = o->ctas > 0 ? std::min(o->ctas, dev->sms) : dev->sms;
+  const int cl = o->cluster > 1 ? o->cluster : 1;
+  if (cl > kMaxCluster || (cl & (cl - 1)) != 0)
+    return fail(PERKS_ERR_INVALID_ARG, "cluster must be 1, 2, 4, 8 or 16");
+  if (cl > 1 && o->kernel != PERKS_KERNEL_PERSISTENT)
+    return fail(PERKS_ERR_INVALID_ARG, "clusters are an option of the persistent kernel");
+  int ctas_used = ctas;
   const size_t vbytes = (size_t(n) * ws + 255) & ~size_t(255);
   const size_t nval = A.fmt == 0 ? size_t(A.nnz) : size_t(A.ndiag) * n;
   constexpr size_t kTail = 80 * 1024;   // partial sums (4 slots x 2 x 1024 CTAs) + scalars
@@ -1547,8 +1644,41 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
     PERKS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCgThreads, dsmem));
     if (per_sm < 1) return fail(PERKS_ERR_LAUNCH, "CG kernel does not fit on an SM");
     void* args[] = {&P};
-    cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(ctas), dim3(kCgThreads), args, dsmem, s);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchCooperativeKernel(cg)");
+    cudaError_t e;
+    if (cl > 1) {
+      // cooperative launch (every CTA resident, for the grid barrier) in
+      // thread-block clusters of `cl` CTAs; the grid is as many whole
+      // clusters as can be resident at once
+      cudaLaunchAttribute at[2];
+      at[0].id = cudaLaunchAttributeCooperative;
+      at[0].val.cooperative = 1;
+      at[1].id = cudaLaunchAttributeClusterDimension;
+      at[1].val.clusterDim.x = unsigned(cl);
+      at[1].val.clusterDim.y = 1;
+      at[1].val.clusterDim.z = 1;
+      cudaLaunchConfig_t cfg{};
+      cfg.blockDim = dim3(kCgThreads);
+      cfg.dynamicSmemBytes = dsmem;
+      cfg.stream = s;
+      cfg.attrs = at;
+      cfg.numAttrs = 2;
+      if (cl > 8) PERKS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      cfg.gridDim = dim3(unsigned(ctas / cl * cl));
+      int maxcl = 0;
+      e = cudaOccupancyMaxActiveClusters(&maxcl, kern, &cfg);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveClusters(cg)");
+      const int grid = std::min(ctas / cl, maxcl) * cl;
+      if (grid < cl) return fail(PERKS_ERR_UNSUPPORTED, "no cluster of " + std::to_string(cl) + " CTAs fits");
+      cfg.gridDim = dim3(unsigned(grid));
+      P.cluster = cl;
+      e = cudaLaunchKernelExC(&cfg, kern, args);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchKernelExC(cg, cooperative clusters)");
+      ctas_used = grid;
+    } else {
+      P.cluster = 1;
+      e = cudaLaunchCooperativeKernel(kern, dim3(ctas), dim3(kCgThreads), args, dsmem, s);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchCooperativeKernel(cg)");
+    }
     launches = 1;
   } else {
     // one launch per phase; scalars on the device; the host checks the
@@ -1659,6 +1789,7 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
     res->ms = ms;
     res->launches = launches;
     res->layout = P.A.fmt;
+    res->ctas = ctas_used;
   }
   const double thr = o->stop == PERKS_STOP_REL ? o->tol * o->tol * tr[1] : o->tol * o->tol;
   if (!o->static_iter && iters >= o->max_iter && !(rr < thr))
@@ -1687,6 +1818,7 @@ void perks_cg_default_opts(perks_cg_opts* o) {
   o->stream = nullptr;
   o->checkpoint = nullptr;
   o->cache_vectors = -1;
+  o->cluster = 1;
 }
 
 int perks_cg_csr(int n, int nnz, const int* rp, const int* ci, const void* val, const void* b, void* x,

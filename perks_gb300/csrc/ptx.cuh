@@ -147,6 +147,60 @@ __device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// ----------------------------------------------------------------- clusters
+// Thread-block cluster helpers: rank of this CTA in its cluster, the
+// cluster's index in the grid, distributed shared memory (DSMEM) access to a
+// peer CTA's shared memory (mapa + ld/st.shared::cluster), and the cluster
+// barrier (every thread of every CTA of the cluster arrives, then waits; the
+// release/acquire pair orders the memory accesses made before the arrival).
+__device__ __forceinline__ unsigned cluster_ctarank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cluster_nctarank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cluster_index_x() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cluster_count_x() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+  return r;
+}
+// Shared-memory address of `p` (this CTA's variable) in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t dsmem_addr(const void* p, unsigned rank) {
+  uint32_t out;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(out) : "r"(smem_u32(p)), "r"(rank));
+  return out;
+}
+__device__ __forceinline__ void dsmem_st_f64(uint32_t addr, double v) {
+  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(addr), "d"(v) : "memory");
+}
+__device__ __forceinline__ double dsmem_ld_f64(uint32_t addr) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ void dsmem_st_u32(uint32_t addr, unsigned v) {
+  asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned dsmem_ld_u32(uint32_t addr) {
+  unsigned v;
+  asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+  return v;
+}
+// (Not the .aligned form: the threads of a warp may arrive after divergent
+// branches, e.g. one thread that waited at the grid barrier.)
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
 // ------------------------------------------------------------- grid barrier
 // Barrier over all CTAs of a cooperative launch on a monotonically increasing
 // arrival counter (bar[0], zeroed before the launch): the k-th barrier
@@ -168,14 +222,25 @@ struct GridBarrier {
     epoch++;
     __syncthreads();
     if (threadIdx.x == 0) {
-      unsigned ok = 1;
-      const unsigned target = epoch * nblocks;
-      unsigned old;
       // The fence publishes the whole CTA's writes (ordered before it by the
       // __syncthreads); acq_rel makes the last arriver, which does not spin,
       // acquire the other CTAs' writes too (L1 may hold stale lines otherwise).
       __threadfence();
-      bool skip = epoch == 1 && int(blockIdx.x) == ctl.skip_cta;
+      s_ok = arrive_wait(int(blockIdx.x)) ? 1u : 0u;
+    }
+    __syncthreads();
+    return s_ok != 0;
+  }
+
+  // One thread's arrival and bounded wait for the `epoch`-th completion
+  // (epoch already counted by the caller); `me` is the arriving unit's index
+  // for the test hook. The caller has fenced its unit's writes.
+  __device__ __forceinline__ bool arrive_wait(int me) {
+    {
+      unsigned ok = 1;
+      const unsigned target = epoch * nblocks;
+      unsigned old;
+      bool skip = epoch == 1 && me == ctl.skip_cta;
       if (skip) {
         // test hook: this CTA does not arrive, so at most nblocks - 1 arrivals
         // come and every CTA's wait (its own included) runs out its budget
@@ -198,10 +263,8 @@ struct GridBarrier {
         }
       }
       if (ok && *((volatile unsigned*)status) != 0u) ok = 0;
-      s_ok = ok;
+      return ok != 0;
     }
-    __syncthreads();
-    return s_ok != 0;
   }
 };
 

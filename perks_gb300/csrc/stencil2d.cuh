@@ -226,8 +226,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
   const int edge_col = lane < H ? max(x0 - 1 - lane, 0) : min(x0 + SW + (lane - H), wx - 1);
   const int edge_chunk = (edge_col / V16) * V16;
   const int edge_sub = edge_col - edge_chunk;
-  constexpr int VS = 32 * V16;                           // vector stride of the shared-memory rows
-  T* const my_ring_v = ring + lane * V16;                 // this lane's first vector in a slot (vector-major)
+  T* const my_ring_v = ring + lane * V;                   // this lane's columns in a slot
   T* const my_ring_e = ring + SW + min(lane, 2 * H - 1) * V16;  // this edge lane's chunk in a slot
   // Shuffle sources and selectors of the horizontal window (row independent).
   int src_l[H], src_r[H];
@@ -246,7 +245,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
   const F2 one2(p.one);
   bool ok = true;
 
-  auto res_ptr = [&](int r) -> T* { return res + (size_t(r - rres0) * NW + wid) * SW + lane * V16; };
+  auto res_ptr = [&](int r) -> T* { return res + (size_t(r - rres0) * NW + wid) * SW + lane * V; };
   auto is_res = [&](int r) { return r >= rres0 && r < rres0 + C; };
 
   if (C > 0) {
@@ -254,7 +253,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
     for (int k = 0; k < C; k++) {
       T v[V];
       load_lane<NV>(fin + size_t(rres0 + k) * pitch + xl, v);
-      store_lane<NV, VS>(res_ptr(rres0 + k), v);
+      store_lane<NV>(res_ptr(rres0 + k), v);
     }
   }
 
@@ -279,7 +278,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
           if (!is_res(r)) {
             const uint64_t pl = (alt && interior(r)) ? pol_first : pol;
 #pragma unroll
-            for (int k = 0; k < NV; k++) cp_async16(my_ring_v + size_t(sf) * SLOT + k * VS, src + xl + k * V16, pl);
+            for (int k = 0; k < NV; k++) cp_async16(my_ring_v + size_t(sf) * SLOT + k * V16, src + xl + k * V16, pl);
           }
           if (edge_lane) cp_async16(slot + SW + lane * V16, src + edge_chunk, pol);
         }
@@ -291,7 +290,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
         RowT out;
         const int r = row_of(q);
         const bool rr = is_res(r);
-        load_lane<NV, VS>(rr ? res_ptr(r) : my_ring_v + size_t(sl) * SLOT, out.v);
+        load_lane<NV>(rr ? res_ptr(r) : my_ring_v + size_t(sl) * SLOT, out.v);
         out.e = edge_lane ? my_ring_e[size_t(sl) * SLOT + edge_sub] : T(0);
         if (ghost_strip) {
           // elements beyond the last column take that column's value
@@ -399,7 +398,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
         }
         T* dst = fout + size_t(y) * pitch + xl;
         if (is_res(y)) {
-          store_lane<NV, VS>(res_ptr(y), o);
+          store_lane<NV>(res_ptr(y), o);
           if (lane * V < H || (lane + 1) * V > SW - H) store_lane<NV>(dst, o);
         } else {
           store_lane<NV>(dst, o);
@@ -461,7 +460,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
     T* fnew = static_cast<T*>(p.f[(p.t0 + p.steps) & 1]);
     for (int k = 0; k < C; k++) {
       T v[V];
-      load_lane<NV, VS>(res_ptr(rres0 + k), v);
+      load_lane<NV>(res_ptr(rres0 + k), v);
       store_lane<NV>(fnew + size_t(rres0 + k) * pitch + xl, v);
     }
   }

@@ -193,3 +193,33 @@ def test_cg_csr_layouts(native, cuda, oracle, layout, expect, dtype):
         assert it_close(res["iterations"], it), (layout, res, it)
     assert res["true_rel_res"] <= 1e-10 * 1.05
     assert true_rel(rp, ci, v, b, x.cpu().numpy()) <= 1e-10 * 1.05
+
+
+@pytest.mark.parametrize("cluster", [2, 4, 8])
+@pytest.mark.parametrize("matrix,dtype", [("lap2d", "fp64"), ("spd", "fp64"), ("lap2d", "mixed"), ("spd", "fp32")])
+def test_cg_cluster_combine(native, cuda, oracle, cluster, matrix, dtype):
+    """Grid reductions through thread-block clusters (partials combined over
+    distributed shared memory, one grid-barrier arrival per cluster): the
+    same convergence as the oracle, whole clusters, and the same result on a
+    second run (the combine order is fixed)."""
+    from perks_gb300 import matrices as M
+    rp, ci, v = M.laplacian_2d(96) if matrix == "lap2d" else M.random_spd(20000, 3)
+    b = np.random.default_rng(8).uniform(-1, 1, len(rp) - 1)
+    if dtype == "fp32":
+        v32, b32 = v.astype(np.float32), b.astype(np.float32)
+        xo, _, _, _ = oracle.cg(rp, ci, v32, b32, max_iter=10, static_iter=True)
+        xs = [native.cg_csr(rp, ci, v32, b32, dtype="fp32", max_iter=10, static_iter=True, cluster=cluster,
+                            device=cuda) for _ in range(2)]
+        assert xs[0][1]["ctas"] % cluster == 0
+        assert np.array_equal(xs[0][0].cpu().numpy(), xs[1][0].cpu().numpy())
+        xg = xs[0][0].cpu().numpy().astype(np.float64)
+        assert np.linalg.norm(xg - xo) <= 1e-4 * np.linalg.norm(xo)
+        return
+    _, it, _, _ = oracle.cg(rp, ci, v, b, max_iter=20000, stop=1, tol=1e-10)
+    runs = [native.cg_csr(rp, ci, v, b, dtype=dtype, tol=1e-10, cluster=cluster, device=cuda) for _ in range(2)]
+    (x, res), (x2, res2) = runs
+    assert res["ctas"] % cluster == 0 and res["ctas"] >= cluster
+    assert np.array_equal(x.cpu().numpy(), x2.cpu().numpy()) and res["iterations"] == res2["iterations"]
+    if dtype == "fp64":
+        assert it_close(res["iterations"], it), (res, it)
+    assert true_rel(rp, ci, v, b, x.cpu().numpy()) <= 1e-10 * 1.05

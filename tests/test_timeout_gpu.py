@@ -49,16 +49,18 @@ def test_stencil_barrier_timeout(native, cuda, oracle, shape, dims, dt, skip_cta
     assert bits_equal(g, oracle.stencil(shape, f, 4))
 
 
-@pytest.mark.parametrize("dtype", ["fp64", "mixed", "fp32"])
-def test_cg_barrier_timeout(native, cuda, oracle, dtype):
+@pytest.mark.parametrize("dtype,cluster", [("fp64", 1), ("mixed", 1), ("fp32", 1), ("fp64", 4), ("mixed", 8)])
+def test_cg_barrier_timeout(native, cuda, oracle, dtype, cluster):
+    """With clusters the hook makes one cluster's leader skip its arrival;
+    every cluster barrier is still passed by all CTAs of a cluster."""
     from perks_gb300 import matrices as M
     rp, ci, v = M.laplacian_2d(64)
     b = np.random.default_rng(4).uniform(-1, 1, len(rp) - 1)
     tol = 1e-5 if dtype == "fp32" else 1e-10
     with wait_fault(native, skip_cta=3):
-        x, res = native.cg_csr(rp, ci, v, b, dtype=dtype, tol=tol, device=cuda, check=False)
+        x, res = native.cg_csr(rp, ci, v, b, dtype=dtype, tol=tol, device=cuda, check=False, cluster=cluster)
     assert res["status"] == TIMEOUT, native.last_error()
-    x, res = native.cg_csr(rp, ci, v, b, dtype=dtype, tol=tol, device=cuda)
+    x, res = native.cg_csr(rp, ci, v, b, dtype=dtype, tol=tol, device=cuda, cluster=cluster)
     assert res["status"] == 0
     if dtype == "fp64":
         _, it, _, _ = oracle.cg(rp, ci, v, b, max_iter=20000, stop=1, tol=1e-10)
