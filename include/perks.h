@@ -232,9 +232,9 @@ typedef struct {
   int cache_vectors;  /* persistent kernel: KB of shared memory per CTA in which each CTA keeps its
                          rows of the vectors that only it touches (r unless the SpMV gathers it, x
                          or the mixed increment, Ap) for the whole solve; the rest streams.
-                         0 = none, -1 = the library's default (none: the shared memory is taken
-                         from the L1 cache that the SpMV gathers use, and on GB300 that cost more
-                         than it saved) */
+                         0 = none, -1 = the library's default: 160 KB for the DIA and ELL layouts,
+                         none for CSR and SELL (the shared memory is taken from the L1 cache that
+                         the SpMV gathers use: more than about 160 KB cost more than it saved) */
   int cluster;        /* persistent kernel: CTAs per thread-block cluster (1 = none, default; 2, 4,
                          8, 16): the CTAs of a cluster combine their dot-product partials over
                          distributed shared memory and only one CTA per cluster takes part in the

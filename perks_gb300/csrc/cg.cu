@@ -49,6 +49,7 @@
 namespace perks {
 
 constexpr int kCgThreads = 1024;
+constexpr int kCgResidentKB = 160;  // default shared-memory residency budget per CTA (DIA / ELL layouts)
 constexpr int kMaxDiag = 32;
 
 // SELL-C-sigma (Kreutzer et al., "A unified sparse matrix data format for
@@ -1616,15 +1617,17 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
     // (2), Ap (2, not SELL). Each takes its CTA's rows up to what is left of
     // the budget; rows past a cap stream through global memory. The budget
     // is taken from the L1 cache (one 256 KB store per SM), on which the
-    // SpMV gathers depend: measured on GB300, a full carve-out (~220 KB)
-    // made every solve slower (2D Laplacian 2048^2 FP64 130 vs 107 us per
-    // iteration), so the default keeps nothing resident.
+    // SpMV gathers depend. Measured on GB300 (2D Laplacian 2048^2, us per
+    // iteration, FP64 / mixed / FP32): none 110.6 / 61.4 / 54.0, 160 KB
+    // 102.8 / 56.0 / 48.9, the whole ~220 KB 130.3 / 66.5 / 63.8; no effect
+    // on the SELL layout (only x can stay). Default: 160 KB for DIA and ELL.
     cudaFuncAttributes fa{};
     PERKS_CUDA(cudaFuncGetAttributes(&fa, kern));
     const bool gathered_r = ((f32 || mixed) && (f == 1 || f == 2)) || f == 3;
     const size_t es = ws;  // FP64 / FP32; mixed: the FP32 r, x_s, Ap
     const long long most = (long long)dev->smem_optin - (long long)fa.sharedSizeBytes - 256;
-    long long budget = o->cache_vectors > 0 ? std::min<long long>(most, 1024ll * o->cache_vectors) : 0;
+    const int kb = o->cache_vectors >= 0 ? o->cache_vectors : ((f == 1 || f == 2) ? kCgResidentKB : 0);
+    long long budget = std::min<long long>(most, 1024ll * kb);
     // rows of the CTA with the most: DIA/ELL split evenly; CSR (merge path)
     // and SELL (whole 1024-row windows) vary around n / ctas
     const long long even = (n + ctas - 1) / ctas;
