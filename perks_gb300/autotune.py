@@ -7,7 +7,9 @@ ProcessRsts2cuh.py -> perksconfig.cuh). This tool does the same for the
 GB300 kernels and adds a measurement, because here the choices that matter
 change speed without changing registers much. 2D: warps per CTA, rows in
 flight per warp, the form of the exact division, rows per copy wait. 3D:
-compute warps per CTA, rows per compute warp, KB of planes in flight.
+compute warps per CTA, rows per compute warp, KB of planes in flight; 2D
+also the 16-byte vectors each lane holds per row (fewer cells per lane: a
+smaller register window, so more warps fit).
 
   1. compile every candidate of every translation unit of the kind with
      -DPERKS_TUNE_* and -Xptxas -v, in parallel;
@@ -52,7 +54,7 @@ KINDS = {
     "2d": {"prefix": "s2d", "shapes": SHAPES2D, "base": 0, "table": os.path.join(B.CSRC, "tune2d.cuh"),
            "decl": "constexpr Tune2D kTune2D[2][2][8]",
            "knobs": [("nw", "PERKS_TUNE_NW"), ("d", "PERKS_TUNE_D"), ("fin", "PERKS_TUNE_FIN"),
-                     ("rp", "PERKS_TUNE_RP")],
+                     ("rp", "PERKS_TUNE_RP"), ("nv", "PERKS_TUNE_NV")],
            "kernel_re": re.compile(r"Function properties for _ZN5perks16stencil2d_kernelI[fd]Li(\d+)E")},
     "3d": {"prefix": "s3d", "shapes": SHAPES3D, "base": 16, "table": os.path.join(B.CSRC, "tune3d.cuh"),
            "decl": "constexpr Tune3D kTune3D[2][2][5]",
@@ -155,7 +157,7 @@ class Lib:
         return st
 
 
-def measure(kind: str, libs: dict, dtypes, orders, size: int, steps: dict, reps: int) -> dict:
+def measure(kind: str, libs: dict, dtypes, orders, size: int, steps: dict, reps: int, only=()) -> dict:
     import torch
     dev = torch.device("cuda:0")
     stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
@@ -173,6 +175,8 @@ def measure(kind: str, libs: dict, dtypes, orders, size: int, steps: dict, reps:
         for ordn in orders:
             order = N.ORDER_REFERENCE if ordn == "ref" else N.ORDER_FAST
             for shape in KINDS[kind]["shapes"]:
+                if only and shape not in only:
+                    continue
                 key = f"{dtn}/{ordn}/{shape}"
                 libs["default"].run(shape, dt, order, small, o_ref, 7, stream)
                 res = {}
@@ -289,6 +293,8 @@ def main(argv=None) -> int:
     ap.add_argument("--d", default="4,6", help="2D rows in flight per warp")
     ap.add_argument("--fin", default="0,1", help="2D division form (reference order)")
     ap.add_argument("--rp", default="1,2", help="2D rows per copy wait")
+    ap.add_argument("--nv", default="0", help="2D 16-byte vectors per lane (0 = built-in)")
+    ap.add_argument("--shapes", default="", help="only these shapes (comma-separated)")
     ap.add_argument("--nwc", default="6,8,11,15", help="3D compute warps per CTA")
     ap.add_argument("--ry", default="2,3,4", help="3D rows per compute warp")
     ap.add_argument("--dkb", default="72", help="3D KB of planes in flight")
@@ -338,7 +344,8 @@ def main(argv=None) -> int:
     libs = {"default": Lib(B.LIB)}
     for v, p in zip(cands, paths):
         libs[v["name"]] = Lib(p)
-    results = measure(a.kind, libs, dtypes, orders, size, steps, a.reps)
+    results = measure(a.kind, libs, dtypes, orders, size, steps, a.reps,
+                      tuple(s for s in a.shapes.split(",") if s))
     table = choose(results, spills, a.margin, a.kind)
     print(json.dumps(table, indent=1))
     if a.json:

@@ -49,14 +49,16 @@ struct Stencil2DParams {
   float one = 1.0f;  // 1.0 the compiler cannot see (packed FP32 sums, see f32x2.cuh)
 };
 
-// Shape geometry and the built-in choice of warps per CTA.
-template <class T, int SHAPE>
+// Shape geometry and the built-in choice of warps per CTA. NVO overrides the
+// 16-byte vectors per lane (0 = built-in).
+template <class T, int SHAPE, int NVO = 0>
 struct Geom2D {
   static constexpr int H = ShapeInfo<SHAPE>::H;
   static constexpr bool BOX = ShapeInfo<SHAPE>::box;
   static constexpr int V16 = 16 / sizeof(T);             // elements per 16-byte vector
-  // vectors per lane per row (one for the widest FP64 windows, to fit registers)
-  static constexpr int NV = (sizeof(T) == 8 && H >= 5) ? 1 : 2;
+  // vectors per lane per row (built-in: one for the widest FP64 windows, to
+  // fit registers; the measured table may choose one for wide FP32 windows)
+  static constexpr int NV = NVO ? NVO : (sizeof(T) == 8 && H >= 5) ? 1 : 2;
   static constexpr int V = NV * V16;                     // elements per lane (8 FP32 / 4 FP64)
   static constexpr int SW = 32 * V;                      // strip width
   static constexpr int WN = 2 * H + 1;                   // window rows
@@ -74,21 +76,27 @@ struct Geom2D {
   static constexpr bool PAIR = sizeof(T) == 4 && !BOX && SHAPE <= PERKS_2DS25PT;
 };
 
-// Warps per CTA, rows in flight, division form and rows per copy wait for one kernel: the
-// measured table (tune2d.cuh), else the built-in choice. The tuning tool
-// overrides all three for a whole translation unit with PERKS_TUNE_*.
+// Warps per CTA, rows in flight, division form, rows per copy wait and
+// vectors per lane for one kernel: the measured table (tune2d.cuh), else the
+// built-in choice. The tuning tool overrides them for a whole translation
+// unit with PERKS_TUNE_*.
 template <class T, int SHAPE, bool FAST>
 struct Pick2D {
   static constexpr Tune2D t = kTune2D[sizeof(T) == 8][FAST][SHAPE];
+#ifdef PERKS_TUNE_NV
+  static constexpr int NVC = PERKS_TUNE_NV;
+#else
+  static constexpr int NVC = t.nv;  // 0 = built-in
+#endif
 #ifdef PERKS_TUNE_NW
   static constexpr int NW = PERKS_TUNE_NW;
 #else
-  static constexpr int NW = t.nw ? t.nw : Geom2D<T, SHAPE>::NW_DEF;
+  static constexpr int NW = t.nw ? t.nw : Geom2D<T, SHAPE, NVC>::NW_DEF;
 #endif
 #ifdef PERKS_TUNE_D
   static constexpr int D = PERKS_TUNE_D;
 #else
-  static constexpr int D = t.d ? t.d : Geom2D<T, SHAPE>::d_def(NW);
+  static constexpr int D = t.d ? t.d : Geom2D<T, SHAPE, NVC>::d_def(NW);
 #endif
 #ifdef PERKS_TUNE_FIN
   static constexpr int FIN = FAST ? 0 : PERKS_TUNE_FIN;
@@ -104,9 +112,9 @@ struct Pick2D {
 
 // Full configuration. The chosen values are template arguments, so kernels
 // built with different choices never share a name.
-template <class T, int SHAPE, int NW_, int D_, int FIN_, int RP_>
-struct Cfg2DT : Geom2D<T, SHAPE> {
-  using G = Geom2D<T, SHAPE>;
+template <class T, int SHAPE, int NW_, int D_, int FIN_, int RP_, int NV_ = 0>
+struct Cfg2DT : Geom2D<T, SHAPE, NV_> {
+  using G = Geom2D<T, SHAPE, NV_>;
   static constexpr int NW = NW_;
   static constexpr int NT = NW * 32;
   static constexpr int D = D_;                           // rows in flight per warp
@@ -122,7 +130,7 @@ struct Cfg2DT : Geom2D<T, SHAPE> {
 };
 template <class T, int SHAPE, bool FAST = false>
 using Cfg2D = Cfg2DT<T, SHAPE, Pick2D<T, SHAPE, FAST>::NW, Pick2D<T, SHAPE, FAST>::D, Pick2D<T, SHAPE, FAST>::FIN,
-                    Pick2D<T, SHAPE, FAST>::RP>;
+                    Pick2D<T, SHAPE, FAST>::RP, Pick2D<T, SHAPE, FAST>::NVC>;
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, uint64_t pol) {
   asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(smem_u32(smem)), "l"(gmem),
