@@ -42,14 +42,15 @@ def test_choose_needs_a_wider_margin_to_spill_more():
 def test_write_table_roundtrip(tmp_path):
     dst = tmp_path / "tune2d.cuh"
     shutil.copy(A.TABLE, dst)
-    t = {"f32/ref/2ds9pt": {"nw": 16, "d": 4, "fin": 1, "rp": 2}, "f64/fast/2d25pt": {"nw": 8, "d": 3, "fin": 0, "rp": 0}}
+    t = {"f32/ref/2ds9pt": {"nw": 16, "d": 4, "fin": 1, "rp": 2, "nv": 1},
+         "f64/fast/2d25pt": {"nw": 8, "d": 3, "fin": 0, "rp": 0, "nv": 0}}
     A.write_table(t, str(dst))
     text = dst.read_text()
     body = text[text.index("// BEGIN TABLE"):text.index("// END TABLE")]
     rows = [r for r in body.split("\n") if "{" in r]
     # f32 ref row, second shape; f64 fast row, last shape
-    assert "{0, 0, 0, 0}, {16, 4, 1, 2}, {0, 0, 0, 0}" in rows[1]
-    assert rows[-1].rstrip().endswith("{8, 3, 0, 0}}}};")
+    assert "{0, 0, 0, 0, 0}, {16, 4, 1, 2, 1}, {0, 0, 0, 0, 0}" in rows[1]
+    assert rows[-1].rstrip().endswith("{8, 3, 0, 0, 0}}}};")
     assert text.count("{") - text.count("}") == 0
     assert A.read_table(str(dst)) == t
 
@@ -57,14 +58,14 @@ def test_write_table_roundtrip(tmp_path):
 def test_merge_keeps_entries_without_a_winner(tmp_path):
     dst = tmp_path / "tune2d.cuh"
     shutil.copy(A.TABLE, dst)
-    A.write_table({"f32/ref/2d5pt": {"nw": 16, "d": 4, "fin": 1, "rp": 0},
-                   "f64/ref/2d21pt": {"nw": 12, "d": 6, "fin": 0, "rp": 0}}, str(dst))
+    A.write_table({"f32/ref/2d5pt": {"nw": 16, "d": 4, "fin": 1, "rp": 0, "nv": 0},
+                   "f64/ref/2d21pt": {"nw": 12, "d": 6, "fin": 0, "rp": 0, "nv": 0}}, str(dst))
     assert A.read_table(str(dst))["f64/ref/2d21pt"]["nw"] == 12
     # a new measurement against the table's kernels: only 2ds9pt has a winner
-    m = A.merge_table(str(dst), "2d", {"f32/ref/2ds9pt": {"nw": 12, "d": 6, "fin": 0, "rp": 2, "gcells": 1.0}})
-    assert m["f32/ref/2d5pt"] == {"nw": 16, "d": 4, "fin": 1, "rp": 0}
-    assert m["f32/ref/2ds9pt"] == {"nw": 12, "d": 6, "fin": 0, "rp": 2}
-    assert m["f64/ref/2d21pt"] == {"nw": 12, "d": 6, "fin": 0, "rp": 0}
+    m = A.merge_table(str(dst), "2d", {"f32/ref/2ds9pt": {"nw": 12, "d": 6, "fin": 0, "rp": 2, "nv": 1, "gcells": 1.0}})
+    assert m["f32/ref/2d5pt"] == {"nw": 16, "d": 4, "fin": 1, "rp": 0, "nv": 0}
+    assert m["f32/ref/2ds9pt"] == {"nw": 12, "d": 6, "fin": 0, "rp": 2, "nv": 1}
+    assert m["f64/ref/2d21pt"] == {"nw": 12, "d": 6, "fin": 0, "rp": 0, "nv": 0}
 
 
 def test_3d_table_roundtrip(tmp_path):
