@@ -141,15 +141,24 @@ __device__ __forceinline__ int cg_split(const CgMat& A, int c, int ncta) {
   return lo;
 }
 
-// SELL SpMV over slices [s0, s1): warp w of the CTA takes slices s0 + w,
-// s0 + w + nwarps, ...; lane l computes the row of slot l in CSR entry order
-// (padding entries add fma(0, x_row, acc) = acc: the sum is never -0) and
-// runs epi(row, sum) for a slot that holds a row.
+// SELL SpMV over slices [s0, s1); lane l computes the row of slot l in CSR
+// entry order (padding entries add fma(0, x_row, acc) = acc: the sum is
+// never -0) and runs epi(row, sum) for a slot that holds a row. The slices of
+// a window are sorted longest first, so with one warp per slice of a window
+// (32 warps, 32 slices per window) warp w takes slice w of even windows and
+// slice 31 - w of odd ones: every warp gets long and short slices alike (a
+// plain round-robin gave warp 0 the longest slice of every window, and the
+// CTA waited for it). Fixed assignment, so the partial sums are reproducible.
 template <class XV, class MV, class XF, class Epi>
 __device__ __forceinline__ void sell_rows(const CgMat& A, const MV* __restrict__ val, int s0, int s1, const XF& xv,
                                           Epi&& epi) {
-  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int s = s0 + (threadIdx.x >> 5); s < s1; s += nw) {
+  constexpr int SPW = kSellWindow / 32;  // slices per window
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5, w = threadIdx.x >> 5;
+  const bool snake = nw == SPW;
+  const int first = snake ? s0 / SPW : s0 + w, last = snake ? (s1 - 1) / SPW : s1 - 1, stride = snake ? 1 : nw;
+  for (int it = first; it <= last; it += stride) {
+    const int s = snake ? it * SPW + ((it & 1) ? SPW - 1 - w : w) : it;
+    if (s < s0 || s >= s1) continue;
     const int e0 = __ldg(A.sl_ptr + s), e1 = __ldg(A.sl_ptr + s + 1);
     const int row = __ldg(A.sl_row + s * 32 + lane);
     XV acc = XV(0);
