@@ -486,6 +486,9 @@ def extra_cg(P, torch):
                 x, res = P.cg_dia(off, data, b, dtype=dt, tol=1e-10)
                 mb = cg_bytes_dia(len(b), len(off), dt)
             out[f"cg_lap2d_2048_{fmt}_{dt}"] = cg_summary(res, mb)
+    # single-reduction CG (one barrier + one two-value reduction per iteration)
+    x, res = P.cg_dia(off, data, b, dtype="fp64", tol=1e-10, algorithm="single_reduction")
+    out["cg_lap2d_2048_dia_fp64_single_reduction"] = cg_summary(res, cg_bytes_dia(len(b), len(off), "fp64"))
     # 3D 7-point Laplacian 160^3 (4.1M rows), CSR input
     rp, ci, v = M.laplacian_3d(160)
     b = np.random.default_rng(1).uniform(-1, 1, len(rp) - 1)
@@ -510,6 +513,9 @@ def extra_cg_spd_sizes(P, torch):
             P.cg_csr(rp, ci, v, b, dtype=dt, tol=1e-10)  # first call: setup of this size
             x, res = P.cg_csr(rp, ci, v, b, dtype=dt, tol=1e-10)
             out[f"cg_spd_{tag}_csr_{dt}"] = cg_summary(res, cg_bytes_csr(n, len(ci), dt))
+        if tag == "1e6":
+            x, res = P.cg_csr(rp, ci, v, b, dtype="fp64", tol=1e-10, algorithm="single_reduction")
+            out["cg_spd_1e6_csr_fp64_single_reduction"] = cg_summary(res, cg_bytes_csr(n, len(ci), "fp64"))
     return out
 
 

@@ -186,6 +186,14 @@ typedef enum {
   PERKS_STOP_REL = 1     /* stop when ||r|| / ||b|| < tol */
 } perks_cg_stop;
 
+typedef enum {
+  PERKS_CG_PLAIN = 0,            /* the reference's iteration (cg_cpu.cpp:40-81): p, A p, alpha, x, r, beta */
+  PERKS_CG_SINGLE_REDUCTION = 1  /* Chronopoulos & Gear (1989): A p and A r carried by recurrences, one row
+                                    pass, one barrier and one fused reduction of r.r and (A r).r per
+                                    iteration; the same iterates in exact arithmetic, other rounding.
+                                    Persistent kernel, FP64 or FP32, no checkpoint. */
+} perks_cg_algorithm;
+
 /* CG checkpoint: the iteration state between two iterations, so that a
  * solve can stop and later resume exactly where it stopped (the resumed run
  * gives bit-identical x and r to one uninterrupted run with the same options).
@@ -239,6 +247,7 @@ typedef struct {
                          8, 16): the CTAs of a cluster combine their dot-product partials over
                          distributed shared memory and only one CTA per cluster takes part in the
                          grid barrier; the grid is then as many whole clusters as fit at once */
+  int algorithm;      /* perks_cg_algorithm (default PERKS_CG_PLAIN) */
 } perks_cg_opts;
 
 typedef struct {

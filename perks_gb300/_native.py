@@ -31,6 +31,7 @@ CLAMP, DIRICHLET = 0, 1
 ORDER_REFERENCE, ORDER_FAST = 0, 1
 KERNEL_PERSISTENT, KERNEL_PER_STEP, KERNEL_NAIVE = 0, 1, 2
 STOP_ABS_RR, STOP_REL = 0, 1
+CG_PLAIN, CG_SINGLE_REDUCTION = 0, 1
 
 
 class StencilOpts(ctypes.Structure):
@@ -55,7 +56,7 @@ class CgOpts(ctypes.Structure):
     _fields_ = [("dtype", c_int), ("stop", c_int), ("tol", c_double), ("max_iter", c_int),
                 ("static_iter", c_int), ("kernel", c_int), ("replace_every", c_int), ("ctas", c_int),
                 ("stream", c_void_p), ("checkpoint", ctypes.POINTER(CgState)), ("cache_vectors", c_int),
-                ("cluster", c_int)]
+                ("cluster", c_int), ("algorithm", c_int)]
 
 
 class CgResult(ctypes.Structure):

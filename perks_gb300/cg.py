@@ -86,7 +86,7 @@ class CgCheckpoint:
 
 
 def _opts(dtype="fp64", stop="rel", tol=1e-10, max_iter=100000, static_iter=False, kernel="persistent",
-          replace_every=0, ctas=0, stream=None, cache_vectors=-1, cluster=1):
+          replace_every=0, ctas=0, stream=None, cache_vectors=-1, cluster=1, algorithm="plain"):
     o = N.CgOpts()
     N.lib().perks_cg_default_opts(ctypes.byref(o))
     o.dtype = _DT[dtype]
@@ -100,6 +100,7 @@ def _opts(dtype="fp64", stop="rel", tol=1e-10, max_iter=100000, static_iter=Fals
     o.stream = stream
     o.cache_vectors = int(cache_vectors)
     o.cluster = int(cluster)
+    o.algorithm = {"plain": N.CG_PLAIN, "single_reduction": N.CG_SINGLE_REDUCTION}[algorithm]
     return o
 
 

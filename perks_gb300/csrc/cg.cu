@@ -841,6 +841,163 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
 }
 
 // ---------------------------------------------------------------------------
+// Single-reduction CG (Chronopoulos & Gear, "s-step iterative methods for
+// symmetric linear systems", J. Comput. Appl. Math. 25, 1989): the same
+// iterates as plain CG in exact arithmetic, with s = A p and w = A r carried
+// by recurrences, so one iteration needs one row pass, one grid barrier and
+// one reduction of two dot products instead of two passes, a barrier and
+// two reductions:
+//   p = r + beta p;  s = w + beta s;  x += alpha p;  r -= alpha s   (rows)
+//   -- barrier --
+//   w = A r;  gamma = r.r;  delta = w.r                              (SpMV)
+//   -- reduction --
+//   beta' = gamma / gamma_old;  alpha' = gamma / (delta - beta' gamma / alpha)
+// Rounding differs from plain CG: r is updated with the recurred s instead of
+// A p, and alpha comes from delta = (A r).r. The stop test is plain CG's, on
+// gamma = r.r. FP64 or FP32 (scalars formed in FP64, rounded to T). p, s and
+// x are touched only by their owning CTA and keep rows in shared memory as far
+// as P.cap_* allow (cap_r: p, cap_x: x, cap_ap: s); r is gathered by the
+// SpMV and w (SELL) written by other CTAs, so both stay in global memory.
+template <class T, int FMT>
+__global__ void __launch_bounds__(kCgThreads, 1) cg_single_red(const __grid_constant__ CgParams P) {
+  const CgMat& A = P.A;
+  const T* __restrict__ val = static_cast<const T*>(A.val);
+  const T* __restrict__ b = static_cast<const T*>(P.b);
+  T* __restrict__ r = static_cast<T*>(P.r);
+  T* __restrict__ w = static_cast<T*>(P.p[1]);  // w = A r
+  const int G = gridDim.x;
+  const int row0 = cg_split(A, blockIdx.x, G), row1 = cg_split(A, blockIdx.x + 1, G);
+  const int2 sr = cta_slices<FMT>(A);
+  GridSum gs{P.part, GridBarrier{P.bar, P.status, unsigned(P.cluster > 1 ? G / P.cluster : G), P.ctl}, P.cluster};
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const bool xvec = aligned16(P.x);
+  const bool v4 = A.fmt != 0 && (A.n & 3) == 0 && aligned16(val) && aligned16(A.eci);
+  int off = 0;
+  const RowVec<T> PV = row_vec<T>(static_cast<T*>(P.p[0]), P.cap_r, row0, row1, off);
+  const RowVec<T> X = row_vec<T>(static_cast<T*>(P.x), P.cap_x, row0, row1, off);
+  const RowVec<T> S = row_vec<T>(static_cast<T*>(P.Ap), P.cap_ap, row0, row1, off);
+  X.load(row0, row1);
+  __syncthreads();
+
+  // r = b - A x, r.r, b.b
+  T rr_t = T(0), bb_t = T(0);
+  {
+    const T* __restrict__ xg = static_cast<const T*>(P.x);
+    auto init_row = [&](int i, T ax) {
+      const T bi = b[i];
+      const T ri = T(-1) * ax + bi;
+      r[i] = ri;
+      rr_t = fma(ri, ri, rr_t);
+      bb_t = fma(bi, bi, bb_t);
+    };
+    if constexpr (FMT == 3) {
+      sell_rows<T>(A, val, sr.x, sr.y, [xg](int c) { return xg[c]; }, init_row);
+    } else {
+      CG_ROWS(i, { init_row(i, spmv_row<FMT>(A, val, xg, i)); })
+    }
+  }
+  double gamma = double(rr_t), bb = double(bb_t);
+  if (!gs.sum2(0, gamma, bb)) return;
+  // w = A r, delta = w.r (the rows of r this CTA's SpMV produces)
+  auto spmv_w = [&](T& g_t, T& d_t) {
+    auto rg = [&](int c) { return r[c]; };
+    cg_rows_spmv<FMT, T>(A, val, rg, row0, row1, sr, [&](int i) {
+      T wv[4], rv[4];
+      spmv4<T, FMT>(A, val, v4, rg, i, wv);
+      ld4(r + i, rv);
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        g_t = fma(rv[u], rv[u], g_t);
+        d_t = fma(wv[u], rv[u], d_t);
+      }
+      st4(w + i, wv);
+    }, [&](int i, T wi) {
+      const T ri = r[i];
+      w[i] = wi;
+      g_t = fma(ri, ri, g_t);
+      d_t = fma(wi, ri, d_t);
+    });
+  };
+  T g0 = T(0), d0 = T(0);
+  spmv_w(g0, d0);
+  double delta = double(d0), unused = double(g0);
+  if (!gs.sum2(1, delta, unused)) return;
+  const double tol2 = (P.stop == PERKS_STOP_REL) ? P.tol * P.tol * bb : P.tol * P.tol;
+  if (!(delta > 0.0) || !isfinite(delta)) {
+    if (!(gamma < tol2)) {  // a zero residual needs no step
+      if (tid == 0 && blockIdx.x == 0) atomicOr(P.status, kErrBreakdown);
+      return;
+    }
+  }
+  double alpha = gamma / delta, beta = 0.0, gamma_old = gamma;
+  int k = 1;
+  while (true) {
+    if (!P.static_iter && gamma < tol2) break;
+    if (k > P.max_iter) break;
+    const T a = T(alpha), be = T(beta);
+    const bool first = k == 1;
+    cg_rows4(row0, row1, xvec, [&](int i) {
+      T pv[4], sv[4], xv[4], rv[4], wv[4];
+      T* const pi = PV.at(i);
+      T* const si = S.at(i);
+      T* const xi = X.at(i);
+      ld4(r + i, rv);
+      ld4(w + i, wv);
+      ld4(xi, xv);
+      if (!first) {
+        ld4(pi, pv);
+        ld4(si, sv);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        pv[u] = first ? rv[u] : fma(be, pv[u], rv[u]);
+        sv[u] = first ? wv[u] : fma(be, sv[u], wv[u]);
+        xv[u] = fma(a, pv[u], xv[u]);
+        rv[u] = fma(-a, sv[u], rv[u]);
+      }
+      st4(pi, pv);
+      st4(si, sv);
+      st4(xi, xv);
+      st4(r + i, rv);
+    }, [&](int i) {
+      T* const pi = PV.at(i);
+      T* const si = S.at(i);
+      T* const xi = X.at(i);
+      const T pn = first ? r[i] : fma(be, *pi, r[i]);
+      const T sn = first ? w[i] : fma(be, *si, w[i]);
+      *pi = pn;
+      *si = sn;
+      *xi = fma(a, pn, *xi);
+      r[i] = fma(-a, sn, r[i]);
+    });
+    if (!gs.bar()) return;
+    T g_t = T(0), d_t = T(0);
+    spmv_w(g_t, d_t);
+    double gn = double(g_t), dn = double(d_t);
+    if (!gs.sum2(1 + (k & 1), gn, dn)) return;
+    beta = gn / gamma_old;
+    const double den = dn - beta * gn / alpha;
+    gamma_old = gn;
+    gamma = gn;
+    k++;
+    if (!P.static_iter && gamma < tol2) break;
+    if (!(den > 0.0) || !isfinite(den)) {
+      if (tid == 0 && blockIdx.x == 0) atomicOr(P.status, kErrBreakdown);
+      return;
+    }
+    alpha = gn / den;
+  }
+  X.store(row0, row1);
+  if (blockIdx.x == 0 && tid == 0) {
+    *P.out_iter = k - 1;
+    P.out_rr[0] = gamma;
+    P.out_rr[1] = 0.0;
+    P.out_rr[2] = bb;
+    *P.out_outer = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Mixed precision: FP32 Krylov iteration, FP64 solution and true residual.
 // Shared-memory residency as in cg_persistent: the FP32 r (unless the SpMV
 // gathers it), the FP32 increment x_s and Ap keep the CTA's rows on chip.
@@ -1367,6 +1524,12 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
     return fail(PERKS_ERR_INVALID_ARG, "unknown kernel kind");
   if (o->dtype == PERKS_MIXED && o->kernel != PERKS_KERNEL_PERSISTENT)
     return fail(PERKS_ERR_UNSUPPORTED, "mixed precision runs in the persistent kernel only");
+  if (o->algorithm != PERKS_CG_PLAIN && o->algorithm != PERKS_CG_SINGLE_REDUCTION)
+    return fail(PERKS_ERR_INVALID_ARG, "unknown CG algorithm");
+  const bool single_red = o->algorithm == PERKS_CG_SINGLE_REDUCTION;
+  if (single_red && (o->kernel != PERKS_KERNEL_PERSISTENT || o->dtype == PERKS_MIXED || o->checkpoint))
+    return fail(PERKS_ERR_UNSUPPORTED,
+                "the single-reduction CG runs in the persistent kernel, FP64 or FP32, without a checkpoint");
   perks_cg_state* ck = o->checkpoint;
   if (ck) {
     if (!ck->d_r || !ck->d_p || ck->k < 0) return fail(PERKS_ERR_INVALID_ARG, "bad checkpoint");
@@ -1611,7 +1774,12 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
   if (o->kernel == PERKS_KERNEL_PERSISTENT) {
     const int f = P.A.fmt;
     const void* kern =
-        o->dtype == PERKS_MIXED
+        single_red
+            ? (f32 ? (f == 0 ? (const void*)cg_single_red<float, 0> : f == 1 ? (const void*)cg_single_red<float, 1>
+                      : f == 2 ? (const void*)cg_single_red<float, 2> : (const void*)cg_single_red<float, 3>)
+                   : (f == 0 ? (const void*)cg_single_red<double, 0> : f == 1 ? (const void*)cg_single_red<double, 1>
+                      : f == 2 ? (const void*)cg_single_red<double, 2> : (const void*)cg_single_red<double, 3>))
+        : o->dtype == PERKS_MIXED
             ? (f == 0 ? (const void*)cg_mixed<0, 0>
                : f == 2 ? (const void*)cg_mixed<2, 0>
                : f == 3 ? (const void*)cg_mixed<3, 0>
@@ -1647,9 +1815,11 @@ static int cg_solve(CgMat A, const void* b, void* x, const perks_cg_opts* o, per
       budget -= rows * (long long)es;
       return int(rows);
     };
-    P.cap_r = take(!gathered_r);
+    // the single-reduction kernel keeps p, x and s (= A p) instead: all three
+    // are touched by their owning CTA only
+    P.cap_r = take(single_red || !gathered_r);
     P.cap_x = take(true);
-    P.cap_ap = take(f != 3);
+    P.cap_ap = take(single_red || f != 3);
     const size_t dsmem = size_t(P.cap_r + P.cap_x + P.cap_ap) * es;
     PERKS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dsmem)));
     int per_sm = 0;
@@ -1831,6 +2001,7 @@ void perks_cg_default_opts(perks_cg_opts* o) {
   o->checkpoint = nullptr;
   o->cache_vectors = -1;
   o->cluster = 1;
+  o->algorithm = PERKS_CG_PLAIN;
 }
 
 int perks_cg_csr(int n, int nnz, const int* rp, const int* ci, const void* val, const void* b, void* x,

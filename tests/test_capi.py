@@ -140,3 +140,21 @@ def test_checkpoint_of_another_solve_rejected_before_launch(native):
     assert b"rows" in L.perks_last_error()
     st.kernel = N.KERNEL_PER_STEP  # written by the other kernel kind
     assert L.perks_cg_csr(10, 28, fake, fake, fake, fake, fake, ctypes.byref(o), ctypes.byref(res)) == -10
+
+
+def test_single_reduction_cg_unsupported_combinations(native):
+    """The single-reduction CG is a persistent-kernel FP64/FP32 solver without
+    checkpoints: other combinations are refused before any device access."""
+    L = native.lib()
+    N = native._native
+    fake = ctypes.c_void_p(16)
+    res = N.CgResult()
+    for dtype, kernel in ((N.MIXED, N.KERNEL_PERSISTENT), (N.FP64, N.KERNEL_PER_STEP)):
+        o = N.CgOpts()
+        L.perks_cg_default_opts(ctypes.byref(o))
+        o.algorithm, o.dtype, o.kernel = N.CG_SINGLE_REDUCTION, dtype, kernel
+        assert L.perks_cg_csr(10, 28, fake, fake, fake, fake, fake, ctypes.byref(o), ctypes.byref(res)) == -11
+    o = N.CgOpts()
+    L.perks_cg_default_opts(ctypes.byref(o))
+    o.algorithm = 7
+    assert L.perks_cg_csr(10, 28, fake, fake, fake, fake, fake, ctypes.byref(o), ctypes.byref(res)) == -10

@@ -223,3 +223,43 @@ def test_cg_cluster_combine(native, cuda, oracle, cluster, matrix, dtype):
     if dtype == "fp64":
         assert it_close(res["iterations"], it), (res, it)
     assert true_rel(rp, ci, v, b, x.cpu().numpy()) <= 1e-10 * 1.05
+
+
+@pytest.mark.parametrize("matrix", ["lap2d", "lap3d", "spd", "tridiag"])
+@pytest.mark.parametrize("fmt", ["csr", "dia"])
+def test_cg_single_reduction_vs_oracle(native, cuda, oracle, matrix, fmt):
+    """Single-reduction CG (Chronopoulos & Gear): the same iteration count as
+    the FP64 oracle's plain CG (within 1, or 1% for long solves), a true
+    residual below the tolerance recomputed on the host, and the same result
+    on a second run."""
+    from perks_gb300 import matrices as M
+    if matrix == "spd" and fmt == "dia":
+        pytest.skip("random pattern has too many diagonals for DIA")
+    rp, ci, v = {"lap2d": lambda: M.laplacian_2d(96), "lap3d": lambda: M.laplacian_3d(24),
+                 "spd": lambda: M.random_spd(20000, 3),
+                 "tridiag": lambda: oracle.gen_tridiag(20000, 1, np.float64)}[matrix]()
+    b = np.random.default_rng(9).uniform(-1, 1, len(rp) - 1)
+    _, it, _, _ = oracle.cg(rp, ci, v, b, max_iter=20000, stop=1, tol=1e-10)
+    runs = []
+    for _ in range(2):
+        if fmt == "csr":
+            runs.append(native.cg_csr(rp, ci, v, b, dtype="fp64", tol=1e-10, algorithm="single_reduction",
+                                      device=cuda))
+        else:
+            off, data = M.csr_to_dia(rp, ci, v)
+            runs.append(native.cg_dia(off, data, b, dtype="fp64", tol=1e-10, algorithm="single_reduction",
+                                      device=cuda))
+    (x, res), (x2, res2) = runs
+    assert it_close(res["iterations"], it), (matrix, fmt, res, it)
+    assert np.array_equal(x.cpu().numpy(), x2.cpu().numpy())
+    assert true_rel(rp, ci, v, b, x.cpu().numpy()) <= 1e-10 * 1.05
+
+
+def test_cg_single_reduction_fp32_tracks_oracle(native, cuda, oracle):
+    rp, ci, v = oracle.gen_tridiag(5000, 2, np.float32)
+    b = np.ones(5000, np.float32)
+    xo, _, _, _ = oracle.cg(rp, ci, v, b, max_iter=6, static_iter=True)
+    x, res = native.cg_csr(rp, ci, v, b, dtype="fp32", max_iter=6, static_iter=True,
+                           algorithm="single_reduction", device=cuda)
+    assert res["iterations"] == 6
+    assert np.allclose(x.cpu().numpy(), xo, rtol=1e-4, atol=1e-6)
