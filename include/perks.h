@@ -94,6 +94,9 @@ typedef struct {
   int tile_y;      /* 3D only: rows per CTA tile; 0 = auto */
   int ctas;        /* CTAs in the persistent grid; 0 = one per SM */
   void* stream;    /* cudaStream_t; NULL = legacy default stream */
+  int tma;         /* 2D persistent / per-step kernels: 1 = rows reach each warp's ring by TMA tensor
+                      copies (one lane issues, an mbarrier per slot), 0 = per-lane cp.async (default).
+                      The 3D kernels always use tensor copies; the naive kernel none. */
 } perks_stencil_opts;
 
 typedef struct {

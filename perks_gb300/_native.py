@@ -37,7 +37,7 @@ CG_PLAIN, CG_SINGLE_REDUCTION = 0, 1
 class StencilOpts(ctypes.Structure):
     _fields_ = [("shape", c_int), ("dtype", c_int), ("boundary", c_int), ("order", c_int),
                 ("kernel", c_int), ("cache_rows", c_int), ("l2_sweep", c_int), ("tile_x", c_int),
-                ("tile_y", c_int), ("ctas", c_int), ("stream", c_void_p)]
+                ("tile_y", c_int), ("ctas", c_int), ("stream", c_void_p), ("tma", c_int)]
 
 
 class StencilStats(ctypes.Structure):

@@ -13,6 +13,10 @@ PERKS_DECL_2D(f32_ref)
 PERKS_DECL_2D(f32_fast)
 PERKS_DECL_2D(f64_ref)
 PERKS_DECL_2D(f64_fast)
+PERKS_DECL_2D(f32_ref_tma)
+PERKS_DECL_2D(f32_fast_tma)
+PERKS_DECL_2D(f64_ref_tma)
+PERKS_DECL_2D(f64_fast_tma)
 #define PERKS_DECL_3D(sfx)                                                                              \
   int stencil3d_##sfx(int shape, const perks_stencil_opts& o, const void* in, void* out, int h, int wy, \
                       int wx, int steps, perks_stencil_stats* st, bool host_io);
@@ -38,12 +42,20 @@ static int check_opts(const perks_stencil_opts* o, bool want3d) {
   if (o->kernel != PERKS_KERNEL_PERSISTENT && o->kernel != PERKS_KERNEL_PER_STEP &&
       !(o->kernel == PERKS_KERNEL_NAIVE && !want3d))
     return fail(PERKS_ERR_INVALID_ARG, "unknown kernel kind");
+  if (o->tma != 0 && o->tma != 1) return fail(PERKS_ERR_INVALID_ARG, "tma must be 0 or 1");
   return PERKS_OK;
 }
 
 static int run2d(const perks_stencil_opts& o, const void* in, void* out, int wy, int wx, int steps,
                  perks_stencil_stats* st, bool host_io) {
   const bool fast = o.order == PERKS_ORDER_FAST;
+  if (o.tma && o.kernel != PERKS_KERNEL_NAIVE) {
+    if (o.dtype == PERKS_FP32)
+      return fast ? stencil2d_f32_fast_tma(o.shape, o, in, out, wy, wx, steps, st, host_io)
+                  : stencil2d_f32_ref_tma(o.shape, o, in, out, wy, wx, steps, st, host_io);
+    return fast ? stencil2d_f64_fast_tma(o.shape, o, in, out, wy, wx, steps, st, host_io)
+                : stencil2d_f64_ref_tma(o.shape, o, in, out, wy, wx, steps, st, host_io);
+  }
   if (o.dtype == PERKS_FP32)
     return fast ? stencil2d_f32_fast(o.shape, o, in, out, wy, wx, steps, st, host_io)
                 : stencil2d_f32_ref(o.shape, o, in, out, wy, wx, steps, st, host_io);

@@ -185,6 +185,7 @@ extern "C" int perks_stencil2d_noalloc(const perks_stencil_opts* o, const void* 
     return fail(PERKS_ERR_INVALID_ARG, "unknown evaluation order");
   if (o->kernel != PERKS_KERNEL_PERSISTENT && o->kernel != PERKS_KERNEL_PER_STEP)
     return fail(PERKS_ERR_INVALID_ARG, "unknown kernel kind");
+  if (o->tma) return fail(PERKS_ERR_UNSUPPORTED, "perks_stencil2d_noalloc runs the cp.async kernel only (tma = 0)");
   if (!d_in || !d_out) return fail(PERKS_ERR_INVALID_ARG, "null device pointer");
   if (wy <= 0 || wx <= 0 || steps < 0) return fail(PERKS_ERR_INVALID_ARG, "sizes must be positive, steps >= 0");
   if (o->order == PERKS_ORDER_FAST)

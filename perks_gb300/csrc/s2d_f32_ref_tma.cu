@@ -1,0 +1,22 @@
+// 2D stencil kernels fed by TMA tensor copies, instantiated for float storage,
+// reference evaluation order.
+#include "stencil2d_host.cuh"
+
+namespace perks {
+int stencil2d_f32_ref_tma(int shape, const perks_stencil_opts& o, const void* in, void* out, int wy, int wx,
+                          int steps, perks_stencil_stats* st, bool host_io) {
+  const float* i = static_cast<const float*>(in);
+  float* q = static_cast<float*>(out);
+  switch (shape) {
+    case PERKS_2D5PT: return launch_stencil2d<float, PERKS_2D5PT, false, true>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2DS9PT: return launch_stencil2d<float, PERKS_2DS9PT, false, true>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2D13PT: return launch_stencil2d<float, PERKS_2D13PT, false, true>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2D17PT: return launch_stencil2d<float, PERKS_2D17PT, false, true>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2D21PT: return launch_stencil2d<float, PERKS_2D21PT, false, true>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2DS25PT: return launch_stencil2d<float, PERKS_2DS25PT, false, true>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2D9PT: return launch_stencil2d<float, PERKS_2D9PT, false, true>(o, i, q, wy, wx, steps, st, host_io);
+    case PERKS_2D25PT: return launch_stencil2d<float, PERKS_2D25PT, false, true>(o, i, q, wy, wx, steps, st, host_io);
+    default: return fail(PERKS_ERR_INVALID_ARG, "not a 2D shape: " + std::to_string(shape));
+  }
+}
+}  // namespace perks

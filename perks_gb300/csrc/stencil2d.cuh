@@ -9,7 +9,11 @@
 //   Each step the warp sweeps its band row by row. Rows are fetched with
 //   cp.async.cg (16 bytes per lane, plus one 16-byte chunk per edge lane for
 //   the H columns left and right of the strip) into a private ring of DR
-//   shared-memory slots, D rows ahead of use; the vertical window of 2H+1 rows
+//   shared-memory slots, D rows ahead of use. The TMA variant (Cf::TMA)
+//   fetches the same rows with tensor copies instead: one lane of the warp
+//   issues two cp.async.bulk.tensor.2d boxes per row (each half of the strip
+//   with EL margin columns) that complete on the slot's mbarrier, and every
+//   lane waits on that barrier before reading the slot. The vertical window of 2H+1 rows
 //   lives in registers and horizontal neighbours move between lanes by warp
 //   shuffles. Nothing synchronises the block inside a step: warps exchange
 //   halos only through the field in global memory, and steps are separated by
@@ -28,6 +32,7 @@
 // clamped; elements of the last strip beyond width_x take the value of column
 // width_x-1), or Dirichlet (outer H cells keep their input value).
 #pragma once
+#include <cuda.h>
 #include <cstdint>
 #include <type_traits>
 #include "ptx.cuh"
@@ -37,6 +42,8 @@
 namespace perks {
 
 struct Stencil2DParams {
+  CUtensorMap map[2];   // TMA variant: box {HALF, 1} over field 0 / 1 (a half row with its margin)
+  CUtensorMap emap[2];  // TMA variant: box {EL, 1}: the margin columns alone (resident rows)
   void* f[2];        // internal fields, pitch elements per row
   int wy, wx, pitch; // domain and padded row pitch (elements)
   int ns, nb;        // strips and bands
@@ -112,7 +119,7 @@ struct Pick2D {
 
 // Full configuration. The chosen values are template arguments, so kernels
 // built with different choices never share a name.
-template <class T, int SHAPE, int NW_, int D_, int FIN_, int RP_, int NV_ = 0>
+template <class T, int SHAPE, int NW_, int D_, int FIN_, int RP_, int NV_ = 0, bool TMA_ = false>
 struct Cfg2DT : Geom2D<T, SHAPE, NV_> {
   using G = Geom2D<T, SHAPE, NV_>;
   static constexpr int NW = NW_;
@@ -121,16 +128,28 @@ struct Cfg2DT : Geom2D<T, SHAPE, NV_> {
   static constexpr int RP = RP_;                         // rows per copy wait (1 or 2)
   static constexpr int DR = D + RP;                      // ring slots per warp
   static constexpr int FIN = FIN_;                       // division form (divconst.cuh)
-  static constexpr int SLOT = G::SW + 2 * G::H * G::V16; // ring slot: strip row + one chunk per edge lane
-  static constexpr size_t ring_bytes = size_t(NW) * DR * SLOT * sizeof(T);
+  static constexpr bool TMA = TMA_;                      // rows fetched by tensor copies
+  // TMA slot: two half rows [x0-EL, x0+SW/2) and [x0+SW/2, x0+SW+EL), each
+  // padded to a multiple of 128 bytes so that every copy destination is
+  // 128-byte aligned; EL = H rounded up to whole 16-byte vectors, so that
+  // every copy starts on a 16-byte boundary of the row.
+  static constexpr int EL = ((G::H + G::V16 - 1) / G::V16) * G::V16;
+  static constexpr int HALF = G::SW / 2 + EL;
+  static constexpr int HALF_P = ((HALF * int(sizeof(T)) + 127) / 128) * 128 / int(sizeof(T));
+  static constexpr int SLOT = TMA ? 2 * HALF_P : G::SW + 2 * G::H * G::V16;  // cp.async: strip row + one chunk per edge lane
+  static constexpr size_t slots_bytes = size_t(NW) * DR * SLOT * sizeof(T);
+  static constexpr size_t mbar_bytes = TMA ? (size_t(NW) * DR * 8 + 127) / 128 * 128 : 0;  // one mbarrier per slot
+  static constexpr size_t ring_bytes = slots_bytes + mbar_bytes;
   static constexpr size_t res_row_bytes = size_t(NW) * G::SW * sizeof(T);  // one resident row for every warp
   static_assert(2 * G::H <= 32, "edge lanes");
   static_assert(NW >= 1 && NW <= 32 && D >= 1 && D <= 8, "launch shape");
   static_assert(RP == 1 || (RP == 2 && D >= 2), "rows per copy wait");
+  static_assert(!TMA || HALF <= 256, "a tensor-copy box is at most 256 elements wide");
+  static_assert(!TMA || DR <= 32, "slot phase bits");
 };
-template <class T, int SHAPE, bool FAST = false>
+template <class T, int SHAPE, bool FAST = false, bool TMA = false>
 using Cfg2D = Cfg2DT<T, SHAPE, Pick2D<T, SHAPE, FAST>::NW, Pick2D<T, SHAPE, FAST>::D, Pick2D<T, SHAPE, FAST>::FIN,
-                    Pick2D<T, SHAPE, FAST>::RP, Pick2D<T, SHAPE, FAST>::NVC>;
+                    Pick2D<T, SHAPE, FAST>::RP, Pick2D<T, SHAPE, FAST>::NVC, TMA>;
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, uint64_t pol) {
   asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(smem_u32(smem)), "l"(gmem),
@@ -141,6 +160,15 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+// One 2D tensor box global -> shared, completing on `bar` (tx-count).
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar,
+                                            uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cta.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint"
+      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
 }
 
 // Vector loads/stores of a lane's V elements (NV 16-byte vectors), vector k
@@ -234,8 +262,20 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
   const int edge_col = lane < H ? max(x0 - 1 - lane, 0) : min(x0 + SW + (lane - H), wx - 1);
   const int edge_chunk = (edge_col / V16) * V16;
   const int edge_sub = edge_col - edge_chunk;
-  T* const my_ring_v = ring + lane * V;                   // this lane's columns in a slot
-  T* const my_ring_e = ring + SW + min(lane, 2 * H - 1) * V16;  // this edge lane's chunk in a slot
+  // TMA slot: margin EL, then the strip; lanes 16..31 start in the second half
+  constexpr int PADE = Cf::HALF_P - Cf::HALF;
+  T* const my_ring_v = Cf::TMA ? ring + Cf::EL + lane * V + (lane >= 16 ? PADE : 0)
+                               : ring + lane * V;                // this lane's columns in a slot
+  T* const my_ring_e = ring + SW + min(lane, 2 * H - 1) * V16;  // cp.async: this edge lane's chunk in a slot
+  // TMA: slot position of this edge lane's column. A column clamped into the
+  // strip (the domain's first or last column) is taken from the registers
+  // instead, because resident rows copy only the margins.
+  int epos = 0;
+  if (Cf::TMA && edge_lane) {
+    const int l = edge_col - x0 + Cf::EL;
+    epos = l + (l >= Cf::HALF ? PADE : 0);
+  }
+  uint64_t* const mb = reinterpret_cast<uint64_t*>(smem_raw + Cf::slots_bytes) + size_t(wid) * DR;  // TMA
   // Shuffle sources and selectors of the horizontal window (row independent).
   int src_l[H], src_r[H];
   bool use_in_l[H], use_in_r[H];
@@ -252,6 +292,17 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
   const uint64_t pol_first = policy_evict_first();
   const F2 one2(p.one);
   bool ok = true;
+  // TMA: one mbarrier per slot of this warp's ring (one arrival: the issuing
+  // lane's expect_tx); per slot the parity of its next phase and whether a
+  // copy into it is in flight
+  unsigned ph = 0, pend = 0;
+  bool copy_ok = true;
+  if constexpr (Cf::TMA) {
+    if (lane == 0)
+      for (int i = 0; i < DR; i++) mbar_init(&mb[i], 1);
+    fence_mbar_init();
+    __syncwarp();
+  }
 
   auto res_ptr = [&](int r) -> T* { return res + (size_t(r - rres0) * NW + wid) * SW + lane * V; };
   auto is_res = [&](int r) { return r >= rres0 && r < rres0 + C; };
@@ -279,18 +330,41 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
       int sl = 0;  // ring slot of the next position to load into registers
       // Issue the copies for sweep position q (one commit group per position).
       auto fetch = [&](int q) {
-        if (q < TY + H) {
-          const int r = row_of(q);
-          const T* src = fin + size_t(r) * pitch;
-          T* slot = ring + size_t(sf) * SLOT;
-          if (!is_res(r)) {
-            const uint64_t pl = (alt && interior(r)) ? pol_first : pol;
-#pragma unroll
-            for (int k = 0; k < NV; k++) cp_async16(my_ring_v + size_t(sf) * SLOT + k * V16, src + xl + k * V16, pl);
+        if constexpr (Cf::TMA) {
+          // two half rows with their margins; for a resident row only the
+          // margins (the neighbouring strips' edge columns)
+          if (q < TY + H && copy_ok) {
+            const int r = row_of(q);
+            T* slot = ring + size_t(sf) * SLOT;
+            if (lane == 0) {
+              if (!is_res(r)) {
+                const uint64_t pl = (alt && interior(r)) ? pol_first : pol;
+                mbar_arrive_expect_tx(&mb[sf], unsigned(2 * Cf::HALF * sizeof(T)));
+                tma_load_2d(slot, &p.map[t & 1], x0 - Cf::EL, r, &mb[sf], pl);
+                tma_load_2d(slot + Cf::HALF_P, &p.map[t & 1], x0 + SW / 2, r, &mb[sf], pl);
+              } else {
+                mbar_arrive_expect_tx(&mb[sf], unsigned(2 * Cf::EL * sizeof(T)));
+                tma_load_2d(slot, &p.emap[t & 1], x0 - Cf::EL, r, &mb[sf], pol);
+                tma_load_2d(slot + Cf::HALF_P + SW / 2, &p.emap[t & 1], x0 + SW, r, &mb[sf], pol);
+              }
+            }
+            pend |= 1u << sf;
           }
-          if (edge_lane) cp_async16(slot + SW + lane * V16, src + edge_chunk, pol);
+        } else {
+          if (q < TY + H) {
+            const int r = row_of(q);
+            const T* src = fin + size_t(r) * pitch;
+            T* slot = ring + size_t(sf) * SLOT;
+            if (!is_res(r)) {
+              const uint64_t pl = (alt && interior(r)) ? pol_first : pol;
+#pragma unroll
+              for (int k = 0; k < NV; k++)
+                cp_async16(my_ring_v + size_t(sf) * SLOT + k * V16, src + xl + k * V16, pl);
+            }
+            if (edge_lane) cp_async16(slot + SW + lane * V16, src + edge_chunk, pol);
+          }
+          cp_async_commit();
         }
-        cp_async_commit();
         sf = (sf + 1 == DR) ? 0 : sf + 1;
       };
       // Move position q from the ring (or resident storage) into registers.
@@ -298,8 +372,36 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
         RowT out;
         const int r = row_of(q);
         const bool rr = is_res(r);
+        if constexpr (Cf::TMA) {
+          if (copy_ok) {
+            const bool w = __all_sync(0xffffffffu, mbar_wait(&mb[sl], (ph >> sl) & 1u, p.ctl.budget));
+            if (w) {
+              ph ^= 1u << sl;
+              pend &= ~(1u << sl);
+            } else {
+              if (lane == 0) atomicOr(p.status, kErrCopyTimeout);
+              copy_ok = false;
+            }
+          }
+        }
         load_lane<NV>(rr ? res_ptr(r) : my_ring_v + size_t(sl) * SLOT, out.v);
-        out.e = edge_lane ? my_ring_e[size_t(sl) * SLOT + edge_sub] : T(0);
+        if constexpr (Cf::TMA) {
+          out.e = edge_lane ? ring[size_t(sl) * SLOT + epos] : T(0);
+          if (x0 == 0) {  // columns left of the domain clamp to column 0
+            const T c0 = __shfl_sync(0xffffffffu, out.v[0], 0);
+            if (lane < H) out.e = c0;
+          }
+          if (lw < SW) {  // columns right of the domain clamp to its last column, in this strip
+            const int le = lw % V;
+            T cl = out.v[0];
+#pragma unroll
+            for (int i = 1; i < V; i++) cl = (le == i) ? out.v[i] : cl;
+            cl = __shfl_sync(0xffffffffu, cl, lw / V);
+            if (edge_lane && lane >= H && x0 + SW + (lane - H) > wx - 1) out.e = cl;
+          }
+        } else {
+          out.e = edge_lane ? my_ring_e[size_t(sl) * SLOT + edge_sub] : T(0);
+        }
         if (ghost_strip) {
           // elements beyond the last column take that column's value
           const int le = lw % V;
@@ -355,7 +457,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
       for (int q = -H; q < -H + D; q++) fetch(q);
       int qn = -H;  // next position to bring into the window
       static_for<2 * H>([&](auto kc) {
-        cp_async_wait<D - 1>();
+        if constexpr (!Cf::TMA) cp_async_wait<D - 1>();
         __syncwarp();
         bring(qn, kc);
         fetch(qn + D);
@@ -419,7 +521,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
               constexpr int j = decltype(jc)::value;
               const int q = q0 + j;
               if (q < TY) {
-                cp_async_wait<D - 1>();
+                if constexpr (!Cf::TMA) cp_async_wait<D - 1>();
                 __syncwarp();
                 bring(qn, std::integral_constant<int, (j + 2 * H) % WN>{});
                 fetch(qn + D);
@@ -438,7 +540,7 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
               constexpr int j0 = 2 * decltype(pc)::value, j1 = j0 + 1;
               const int q = q0 + j0;
               if (q < TY) {
-                cp_async_wait<D - 2>();
+                if constexpr (!Cf::TMA) cp_async_wait<D - 2>();
                 __syncwarp();
                 bring(qn, std::integral_constant<int, (j0 + 2 * H) % WN>{});
                 fetch(qn + D);
@@ -457,11 +559,29 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
       };
       if (fwd) step_rows(std::true_type{});
       else step_rows(std::false_type{});
-      cp_async_wait<0>();
+      if constexpr (!Cf::TMA) cp_async_wait<0>();
       __syncwarp();
     }
-    if (it + 1 < p.steps && p.persistent) {
+    if constexpr (Cf::TMA) {
+      // this step's stores before the next step's tensor copies read them
+      fence_proxy_async_global();
+      if (!__syncthreads_and(copy_ok)) ok = false;
+    }
+    if (ok && it + 1 < p.steps && p.persistent) {
       if (!gbar.sync()) ok = false;
+    }
+  }
+  if constexpr (Cf::TMA) {
+    // after a failed wait: leave no tensor copy in flight into this CTA's
+    // shared memory (a budget of its own; copies end by themselves)
+    if (pend != 0 && lane == 0) {
+      for (int i = 0; i < DR; i++) {
+        if (!((pend >> i) & 1u)) continue;
+        const long long c0 = clock64();
+        while (!mbar_try_wait(&mb[i], (ph >> i) & 1u)) {
+          if (clock64() - c0 > (1ll << 30)) break;
+        }
+      }
     }
   }
   if (ok && C > 0) {

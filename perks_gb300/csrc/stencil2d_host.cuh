@@ -8,6 +8,7 @@
 
 namespace perks {
 
+int encode_tiled_2d(CUtensorMap* map, bool f64, void* base, int pitch, int rows, int box_x);
 
 inline int ceil_div(long long a, long long b) { return int((a + b - 1) / b); }
 
@@ -44,10 +45,11 @@ int min_domain_rows(const perks_stencil_opts& o, int wx, int* wy) {
 
 // d_in / d_out are device buffers, or host buffers when host_io is set: the
 // field then goes straight between them and the internal pitched fields.
-template <class T, int SHAPE, bool FAST>
+// TMA: rows reach the warps' rings by tensor copies instead of cp.async.
+template <class T, int SHAPE, bool FAST, bool TMA = false>
 int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int wy, int wx, int steps,
                      perks_stencil_stats* st, bool host_io = false) {
-  using Cf = Cfg2D<T, SHAPE, FAST>;
+  using Cf = Cfg2D<T, SHAPE, FAST, TMA>;
   constexpr int H = Cf::H;
   const DeviceInfo* dev = device_info();
   if (!dev) return PERKS_ERR_NO_DEVICE;
@@ -114,6 +116,12 @@ int launch_stencil2d(const perks_stencil_opts& o, const T* d_in, T* d_out, int w
   p.bar = sw.bar;
   p.status = sw.status;
   p.ctl = wait_ctl();
+  if constexpr (Cf::TMA) {
+    for (int i = 0; i < 2; i++) {
+      if ((stt = encode_tiled_2d(&p.map[i], sizeof(T) == 8, p.f[i], pitch, wy, Cf::HALF)) != PERKS_OK) return stt;
+      if ((stt = encode_tiled_2d(&p.emap[i], sizeof(T) == 8, p.f[i], pitch, wy, Cf::EL)) != PERKS_OK) return stt;
+    }
+  }
 
   auto kern = stencil2d_kernel<T, SHAPE, FAST, Cf>;
   PERKS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));

@@ -20,7 +20,7 @@ from . import _native as N
 
 
 def _opts(shape: str, dtype, order="reference", kernel="persistent", boundary="clamp", cache_rows=-1,
-          l2_sweep=False, ctas=0, stream=None) -> N.StencilOpts:
+          l2_sweep=False, ctas=0, stream=None, tma=False) -> N.StencilOpts:
     if shape not in N.SHAPES:
         raise ValueError(f"unknown shape {shape!r}")
     o = N.StencilOpts()
@@ -33,6 +33,7 @@ def _opts(shape: str, dtype, order="reference", kernel="persistent", boundary="c
     o.l2_sweep = int(bool(l2_sweep))
     o.ctas = int(ctas)
     o.stream = stream
+    o.tma = int(bool(tma))
     return o
 
 

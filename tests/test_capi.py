@@ -94,6 +94,13 @@ def test_argument_errors_are_status_codes(native):
     o.order = 7
     assert L.perks_stencil2d(ctypes.byref(o), 1, 1, 4, 4, 1, None) == -10
     assert L.perks_stencil3d(None, 1, 1, 4, 4, 4, 1, None) == -10
+    # the copy-engine switch: 0 or 1; the no-allocation entry point runs cp.async only
+    L.perks_stencil_default_opts(ctypes.byref(o), 0, N.FP32)
+    assert o.tma == 0
+    o.tma = 2
+    assert L.perks_stencil2d(ctypes.byref(o), 1, 1, 4, 4, 1, None) == -10
+    o.tma = 1
+    assert L.perks_stencil2d_noalloc(ctypes.byref(o), 1, 1, 4, 4, 1, None) == -11
 
 
 def test_reference_signature_errors(native):

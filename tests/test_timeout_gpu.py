@@ -49,6 +49,21 @@ def test_stencil_barrier_timeout(native, cuda, oracle, shape, dims, dt, skip_cta
     assert bits_equal(g, oracle.stencil(shape, f, 4))
 
 
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_stencil_tma_barrier_timeout(native, cuda, oracle, dt):
+    """The TMA-fed 2D kernel leaves cleanly when the grid barrier times out
+    (no tensor copy is in flight between steps)."""
+    import torch
+    f = np.random.default_rng(8).random((300, 1100)).astype(dt)
+    t = torch.from_numpy(f).to(cuda)
+    with wait_fault(native, 5):
+        with pytest.raises(native.PerksError) as e:
+            native.stencil2d(t, "2ds9pt", 4, kernel="persistent", tma=True)
+    assert e.value.code == TIMEOUT, str(e.value)
+    g, _ = run(native, cuda, f, "2ds9pt", 4, tma=True)
+    assert bits_equal(g, oracle.stencil("2ds9pt", f, 4))
+
+
 @pytest.mark.parametrize("dtype,cluster", [("fp64", 1), ("mixed", 1), ("fp32", 1), ("fp64", 4), ("mixed", 8)])
 def test_cg_barrier_timeout(native, cuda, oracle, dtype, cluster):
     """With clusters the hook makes one cluster's leader skip its arrival;
