@@ -125,6 +125,7 @@ SIGNATURES = {
     "perks_abi_version": (c_int, []),
     "perks_debug_set_wait_fault": (c_int, [ctypes.c_longlong, c_int]),
     "perks_debug_workspace_allocs": (ctypes.c_longlong, []),
+    "perks_debug_div_check": (c_int, [c_int, c_int, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_uint)]),
     "perks_launch_count": (ctypes.c_longlong, []),
     "perks_reset_launch_count": (None, []),
 }

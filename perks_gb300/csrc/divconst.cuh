@@ -31,10 +31,11 @@
 // results; which one ptxas schedules better differs between stencil shapes,
 // so the 2D kernels take FIN from their measured tuning table.
 //
-// The float version (both forms) is checked against IEEE division for all
-// 2^32 inputs with b = 118, 159, 59, 6 and 2 (zero mismatches, signs of zero
-// included), the double version through the bit-exact stencil tests on
-// subnormal, tiny, huge, infinite and NaN fields.
+// The float version (both forms, per element and on packed pairs) is checked
+// against CUDA's IEEE division for all 2^32 inputs with b = 118 and 159
+// (perks_debug_div_check: zero mismatches, signs of zero included), the
+// double version through the bit-exact stencil tests on subnormal, tiny,
+// huge, infinite and NaN fields.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>

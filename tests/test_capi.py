@@ -165,3 +165,11 @@ def test_single_reduction_cg_unsupported_combinations(native):
     L.perks_cg_default_opts(ctypes.byref(o))
     o.algorithm = 7
     assert L.perks_cg_csr(10, 28, fake, fake, fake, fake, fake, ctypes.byref(o), ctypes.byref(res)) == -10
+
+
+def test_division_check_rejects_unknown_divisor(native):
+    L = native.lib()
+    bad = (ctypes.c_longlong * 2)()
+    assert L.perks_debug_div_check(7, 0, bad, None) == -10
+    assert L.perks_debug_div_check(118, 2, bad, None) == -10
+    assert L.perks_debug_div_check(118, 0, None, None) == -10
