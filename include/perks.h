@@ -87,7 +87,8 @@ typedef struct {
   int order;       /* perks_order */
   int kernel;      /* perks_kernel */
   int cache_rows;  /* persistent kernel: rows (2D) / planes (3D) per CTA kept in shared memory;
-                      -1 = as many as fit, 0 = none */
+                      -1 = as many as fit, 0 = none. Default: -1 for 2D, 0 for 3D (resident
+                      planes are built and tested but measured slower on GB300) */
   int l2_sweep;    /* persistent kernel: alternate the sweep direction each step and drop dead
                       lines from L2, so the rows written last are read first from L2 (1 = on) */
   int tile_x;      /* columns per CTA tile; 0 = auto */
@@ -158,9 +159,9 @@ PERKS_API int perks_jacobi_iterative_f64(int shape, const double* h_in, int widt
 /* Replaces j3d_iterative<float/double> (stencil/3dstencil/common/jacobi_cuda.cuh:6-10).
  * Reference return codes kept: -2 unsupported widths, -4 height too small.
  * getminHeight=1 returns the minimum-domain height without running (h_in and
- * h_out may be NULL); it is 0, the reference's answer for a kernel without a
- * plane cache (j3d.driver.cpp:102-108), because the 3D kernel streams every
- * plane through its TMA ring each step and keeps none on chip. */
+ * h_out may be NULL): perks_stencil3d_min_domain for this shape and dtype
+ * (useSM=0: 0, the reference's answer for a run without a plane cache,
+ * j3d.driver.cpp:102-108). */
 PERKS_API int perks_j3d_iterative_f32(int shape, const float* h_in, int height, int width_y, int width_x,
                             float* h_out, int bdimx, int blkpsm, int iteration, int useSM,
                             int usewarmup, int warmupiteration, int isDoubleTile, int getminHeight);
@@ -176,6 +177,15 @@ PERKS_API int perks_j3d_iterative_f64(int shape, const double* h_in, int height,
  * bands read from the field). Depends on shape, dtype, cache_rows and ctas of
  * `opts`; 0 when the options cache nothing (per-step kernel, cache_rows=0). */
 PERKS_API int perks_stencil2d_min_domain(const perks_stencil_opts* opts, int width_x, int* width_y);
+/* The 3D counterpart (the reference's getminHeight, j3d.driver.cpp:62-144):
+ * writes to *height the largest height of a width_y x width_x field at which
+ * the persistent 3D kernel keeps, between time steps, every plane tile of
+ * every CTA's z-runs in shared memory except the H planes at each end of a
+ * run (those are the halo the neighbouring runs read from the field).
+ * Depends on shape, dtype, order, cache_rows (planes per CTA) and ctas of
+ * `opts`; 0 when no plane tile fits next to the kernel's copy ring or
+ * cache_rows = 0. */
+PERKS_API int perks_stencil3d_min_domain(const perks_stencil_opts* opts, int width_y, int width_x, int* height);
 /* getMinWidthY<REAL>(width_x, bdimx, registers, useSM, blkpsm, isDoubleTile)
  * (stencil/2dstencil/common/jacobi_cuda.cuh:14) with the shape and dtype
  * first: returns that width_y (>= 0) or a negative perks_status. bdimx,

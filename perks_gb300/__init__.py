@@ -6,8 +6,8 @@ this package is its ctypes host mirror.
 """
 from . import _native
 from ._native import PerksError, SHAPES, HALO, lib
-from .stencil import (getMinWidthY, j3d_iterative, jacobi_iterative, last_error, min_domain_2d, stencil2d,
-                      stencil3d)
+from .stencil import (getMinWidthY, j3d_iterative, jacobi_iterative, last_error, min_domain_2d, min_domain_3d,
+                      stencil2d, stencil3d)
 from .cg import CgCheckpoint, cg_csr, cg_dia, spmv_csr, spmv_dia
 from .batch import BatchPlan, cg_job, stencil_job
 

@@ -96,6 +96,7 @@ SIGNATURES = {
     "perks_stencil2d_noalloc": (c_int, [ctypes.POINTER(StencilOpts), c_void_p, c_void_p, c_int, c_int, c_int,
                                         ctypes.POINTER(StencilStats)]),
     "perks_stencil2d_min_domain": (c_int, [ctypes.POINTER(StencilOpts), c_int, ctypes.POINTER(c_int)]),
+    "perks_stencil3d_min_domain": (c_int, [ctypes.POINTER(StencilOpts), c_int, c_int, ctypes.POINTER(c_int)]),
     "perks_get_min_width_y": (c_int, [c_int] * 8),
     "perks_jacobi_iterative_f32": (c_int, [c_int, c_void_p, c_int, c_int, c_void_p] + [c_int] * 8),
     "perks_jacobi_iterative_f64": (c_int, [c_int, c_void_p, c_int, c_int, c_void_p] + [c_int] * 8),

@@ -107,7 +107,10 @@ void perks_stencil_default_opts(perks_stencil_opts* o, int shape, int dtype) {
   o->boundary = PERKS_BOUNDARY_CLAMP;
   o->order = PERKS_ORDER_REFERENCE;
   o->kernel = PERKS_KERNEL_PERSISTENT;
-  o->cache_rows = -1;
+  // 2D: as many resident rows as fit. 3D: no resident planes -- measured
+  // slower on GB300 in every regime (the plane copies stall the kernel's copy
+  // ring more than the saved reads gain); cache_rows > 0 or -1 asks for them.
+  o->cache_rows = is3d(shape) ? 0 : -1;
   o->l2_sweep = 0;
   o->tile_x = 0;
   o->tile_y = 0;
@@ -162,7 +165,14 @@ int perks_jacobi_iterative_f64(int shape, const double* h_in, int wy, int wx, do
 static int j3d_common(int shape, int dtype, const void* h_in, int h, int wy, int wx, void* h_out, int iteration,
                       int useSM, int usewarmup, int warmupiteration, int getminHeight) {
   if (!is3d(shape)) return fail(PERKS_ERR_INVALID_ARG, "not a 3D shape");
-  if (getminHeight) return 0;  // no plane cache: the reference's "no cache version" answer
+  if (getminHeight) {  // the largest height whose every run-interior plane stays on chip (0: none fits)
+    perks_stencil_opts o;
+    perks_stencil_default_opts(&o, shape, dtype);
+    o.cache_rows = useSM ? -1 : 0;
+    int hm = 0;
+    const int rc = perks_stencil3d_min_domain(&o, wy, wx, &hm);
+    return rc == PERKS_OK ? hm : rc;
+  }
   if (!h_in || !h_out) return fail(PERKS_ERR_INVALID_ARG, "null host pointer");
   if (wy <= 0 || wx <= 0) return -2;  // reference: unsupported widths
   if (h <= 0) return -4;              // reference: height too small

@@ -26,6 +26,18 @@
 //   separated by one bounded grid barrier.
 //   With `alternate`, odd steps sweep the segments and their planes in reverse,
 //   so that the planes written last are read first while still in L2.
+//   PERKS caching (persistent launches): up to `kr` planes of one of the
+//   CTA's segments stay in shared memory for the whole launch, each as a
+//   [TY][SW] tile. Only planes no other CTA reads are chosen: at least H
+//   planes away from both ends of the segment's z-run (as the 2D kernel's
+//   bands keep no row within H of their ends). For such a plane the producer warp
+//   copies the resident tile into the slot's TY interior rows itself (16-byte
+//   shared loads and stores) before it arrives on the slot's full barrier, and
+//   the tensor copies bring only the H halo rows above and below and the pad
+//   strips from the field. Its output goes back into the resident tile, and to the field
+//   only where neighbouring tiles read it: the first and last H rows, and the
+//   HP columns at each side (vector 0 of lane 0, vector NV-1 of lane 31). The
+//   full planes are written to the field once, at the end of the launch.
 //
 // Boundary: clamp-to-edge as the reference (plane, row and column indices
 // clamped), or Dirichlet (outer H cells keep their input value). Rows and
@@ -51,6 +63,19 @@ __device__ __forceinline__ void vec16_load(const T* src, T* dst) {
     dst[0] = v.x; dst[1] = v.y;
   }
 }
+// 16-byte shared-memory store that the compiler does not order against other
+// memory accesses (no memory clobber): for the resident plane tiles, which
+// the compute loop writes but never reads, so that the ring loads of later
+// rows may still be scheduled ahead of it. Readers of the tiles sit behind a
+// barrier.
+__device__ __forceinline__ void sts16_unordered(float* dst, const float* v) {
+  asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(smem_u32(dst)), "f"(v[0]), "f"(v[1]), "f"(v[2]),
+               "f"(v[3]));
+}
+__device__ __forceinline__ void sts16_unordered(double* dst, const double* v) {
+  asm volatile("st.shared.v2.f64 [%0], {%1, %2};" ::"r"(smem_u32(dst)), "d"(v[0]), "d"(v[1]));
+}
+
 template <class T>
 __device__ __forceinline__ void vec16_store(T* dst, const T* src) {
   if constexpr (sizeof(T) == 4)
@@ -71,7 +96,9 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
 struct Stencil3DParams {
   CUtensorMap map[2];   // box {SW, TY+2H, 1} over field 0 / 1
   CUtensorMap pmap[2];  // box {HP, TY+2H, 1}: the pad strips
+  CUtensorMap hmap[2];  // box {SW, H, 1}: the halo rows of a resident plane
   void* f[2];
+  int kr;             // resident planes per CTA (0: none)
   int h, wy, wx, px;  // domain and x pitch (elements)
   int gx, gy;         // x-y tile grid
   int steps, t0;
@@ -113,8 +140,9 @@ struct Pick3D {
 
 // Full configuration; the chosen values are template arguments, so kernels
 // built with different choices never share a name.
-template <class T, int SHAPE, int NWC_, int RY_, int DKB_>
+template <class T, int SHAPE, int NWC_, int RY_, int DKB_, bool RES_ = false>
 struct Cfg3DT {
+  static constexpr bool RES = RES_;  // built with resident planes (the launcher picks it when a plane fits)
   static constexpr int H = ShapeInfo<SHAPE>::H;
   static constexpr bool BOX = ShapeInfo<SHAPE>::box;
   static constexpr int V16 = 16 / sizeof(T);
@@ -134,23 +162,27 @@ struct Cfg3DT {
   static constexpr int PLANE = MAIN + 2 * PADSZ;           // slot stride (elements)
   static constexpr unsigned tx_bytes = unsigned((SR * SW + 2 * SR * HP) * sizeof(T));
   static constexpr size_t slot_bytes = size_t(PLANE) * sizeof(T);
-  // planes in flight beyond the 2H+1 being read: about DKB KB, at least 2,
-  // within a 200 KB ring, and at least 1 (a ring larger than shared memory is
-  // refused by the launcher)
+  // planes in flight beyond the 2H+1 being read: about DKB KB (every slot
+  // size of the tables' 72 KB gives at least 2), within a 200 KB ring, and at
+  // least 1 (a ring larger than shared memory is refused by the launcher)
   static constexpr int DMAX = int((200u * 1024u) / slot_bytes) - (2 * H + 1);
-  static constexpr int DWANT = int((unsigned(DKB_) * 1024u + slot_bytes - 1) / slot_bytes) > 2
+  static constexpr int DWANT = int((unsigned(DKB_) * 1024u + slot_bytes - 1) / slot_bytes) > 1
                                    ? int((unsigned(DKB_) * 1024u + slot_bytes - 1) / slot_bytes)
-                                   : 2;
+                                   : 1;
   static constexpr int D = (DMAX < DWANT ? DMAX : DWANT) < 1 ? 1 : (DMAX < DWANT ? DMAX : DWANT);
   static constexpr int NR = 2 * H + 1 + D;                // ring slots
   static constexpr size_t ring_bytes = size_t(NR) * slot_bytes;
   static constexpr size_t smem_bytes = ring_bytes + 2 * NR * sizeof(uint64_t);
+  static constexpr size_t res_offset = (smem_bytes + 127) / 128 * 128;  // resident plane tiles
+  static constexpr size_t res_plane_bytes = size_t(TY) * SW * sizeof(T);
+  // bytes the tensor copies of a resident plane complete: halo rows and pads
+  static constexpr unsigned tx_res_bytes = unsigned((2 * H * SW + 2 * SR * HP) * sizeof(T));
   static_assert(NWC >= 1 && NWC <= 31 && RY >= 1, "launch shape");
   static_assert(H <= V16, "horizontal neighbours are at most one lane away");
   static_assert(SW <= 256 && SR <= 256, "TMA box extent");
 };
-template <class T, int SHAPE, bool FAST = false>
-using Cfg3D = Cfg3DT<T, SHAPE, Pick3D<T, SHAPE, FAST>::NWC, Pick3D<T, SHAPE, FAST>::RY, Pick3D<T, SHAPE, FAST>::DKB>;
+template <class T, int SHAPE, bool FAST = false, bool RES = false>
+using Cfg3D = Cfg3DT<T, SHAPE, Pick3D<T, SHAPE, FAST>::NWC, Pick3D<T, SHAPE, FAST>::RY, Pick3D<T, SHAPE, FAST>::DKB, RES>;
 
 template <class T, int SHAPE, bool FAST, class Cf>
 __global__ void __launch_bounds__(Cf::NT, 1) stencil3d_kernel(const __grid_constant__ Stencil3DParams p) {
@@ -172,6 +204,27 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil3d_kernel(const __grid_const
   const long long total = (long long)p.gx * p.gy * h;
   const long long c_lo = total * blockIdx.x / gridDim.x, c_hi = total * (blockIdx.x + 1) / gridDim.x;
   const int nseg = c_hi > c_lo ? int((c_hi - 1) / h - c_lo / h + 1) : 0;
+  // resident planes: [rz0, rz0 + rn) of tile rtile, the segment with the most
+  // planes that no other CTA reads
+  int rtile = -1, rz0 = 0, rn = 0;
+  if (Cf::RES && p.kr > 0) {
+    for (int k = 0; k < nseg; k++) {
+      const long long tb = c_lo / h + k;
+      const int zl = int(max(c_lo, tb * h) - tb * h), zh = int(min(c_hi, (tb + 1) * h) - tb * h);
+      const int a = zl + H, b = zh - H;
+      const int n = min(p.kr, b - a);
+      if (n > rn) {
+        rn = n;
+        rtile = int(tb);
+        rz0 = a;
+      }
+    }
+  }
+  T* const resb = reinterpret_cast<T*>(smem_raw + Cf::res_offset);  // [rn][TY][SW]
+  auto res_index = [&](int tile, int z) {
+    if constexpr (!Cf::RES) return -1;
+    return (tile == rtile && z >= rz0 && z < rz0 + rn) ? z - rz0 : -1;
+  };
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < NR; i++) {
@@ -179,6 +232,27 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil3d_kernel(const __grid_const
       mbar_init(&empty[i], NWC);
     }
     fence_mbar_init();
+  }
+  // the resident planes' tiles from the input field (each compute warp its
+  // own rows)
+  if (Cf::RES && rn > 0 && !producer) {
+    const T* f0 = static_cast<const T*>(p.f[p.t0 & 1]);
+    const int x0 = (rtile % p.gx) * SW, y0 = (rtile / p.gx) * TY;
+    for (int j = 0; j < rn; j++) {
+      for (int r = wid * RY; r < wid * RY + RY; r++) {
+        if (y0 + r >= wy) break;
+        const T* src = f0 + (size_t(rz0 + j) * wy + y0 + r) * px + x0 + lane * V16;
+        T* dst = resb + (size_t(j) * TY + r) * SW + lane * V16;
+#pragma unroll
+        for (int k2 = 0; k2 < NV; k2++) {
+          if (x0 + k2 * 32 * V16 + lane * V16 < px) {
+            T v[V16];
+            vec16_load(src + k2 * 32 * V16, v);
+            vec16_store(dst + k2 * 32 * V16, v);
+          }
+        }
+      }
+    }
   }
   __syncthreads();
 
@@ -223,11 +297,30 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil3d_kernel(const __grid_const
             }
           }
           const int z = fwd ? z_lo + q : z_hi - 1 - q;
+          const int rj = (Cf::RES && z >= 0 && z < h) ? res_index(tile, z) : -1;
+          if (Cf::RES && rj >= 0) {
+            // the resident tile into the slot's interior rows, by the whole
+            // warp, before the arrival that lets the compute warps read it
+            T* dst = ring + size_t(s) * PLANE + H * SW;
+            const T* src = resb + size_t(rj) * TY * SW;
+            for (int e = lane * V16; e < TY * SW; e += 32 * V16) {
+              T v[V16];
+              vec16_load(src + e, v);
+              vec16_store(dst + e, v);
+            }
+            __syncwarp();
+          }
           if (lane == 0) {
             if (z >= 0 && z < h) {
               T* slot = ring + size_t(s) * PLANE;
-              mbar_arrive_expect_tx(&full[s], Cf::tx_bytes);
-              tma_load_3d(slot, &p.map[t & 1], x0, y0 - H, z, &full[s], pol);
+              if (!Cf::RES || rj < 0) {
+                mbar_arrive_expect_tx(&full[s], Cf::tx_bytes);
+                tma_load_3d(slot, &p.map[t & 1], x0, y0 - H, z, &full[s], pol);
+              } else {  // interior rows from the resident tile, halo rows from the field
+                mbar_arrive_expect_tx(&full[s], Cf::tx_res_bytes);
+                tma_load_3d(slot, &p.hmap[t & 1], x0, y0 - H, z, &full[s], pol);
+                tma_load_3d(slot + (H + TY) * SW, &p.hmap[t & 1], x0, y0 + TY, z, &full[s], pol);
+              }
               tma_load_3d(slot + MAIN, &p.pmap[t & 1], x0 - HP, y0 - H, z, &full[s], pol);
               tma_load_3d(slot + MAIN + PADSZ, &p.pmap[t & 1], x0 + SW, y0 - H, z, &full[s], pol);
             } else {
@@ -329,83 +422,112 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil3d_kernel(const __grid_const
           for (int j = 0; j < NP; j++) pl[j] = plane_ptr(z - H + j);
           const bool zfix = z < H || z >= h - H;
           const int yw = y0 + wid * RY;  // this warp's first row
-          // finish one output row: Dirichlet cells keep the old value, store
-          auto finish = [&](int y, T(&o)[V], const T(&c)[V]) {
-            if (dir) {
-              const bool fixed = zfix || y < H || y >= wy - H;
+          const int rj = res_index(tile, z);
+          // one output plane; RP: the plane is resident (its output goes into
+          // its tile, and to the field only what the neighbouring tiles
+          // read). Instantiated twice, so that the loop of the planes that
+          // stream is the plain one.
+          auto do_plane = [&](auto rpc) {
+            constexpr bool RP = decltype(rpc)::value;
+            // finish one output row: Dirichlet cells keep the old value, store
+            auto finish = [&](int y, T(&o)[V], const T(&c)[V]) {
+              if (dir) {
+                const bool fixed = zfix || y < H || y >= wy - H;
 #pragma unroll
-              for (int i = 0; i < V; i++) {
-                const int x = x0 + col(i);
-                o[i] = (fixed || x < H || x >= wx - H) ? c[i] : o[i];
+                for (int i = 0; i < V; i++) {
+                  const int x = x0 + col(i);
+                  o[i] = (fixed || x < H || x >= wx - H) ? c[i] : o[i];
+                }
               }
-            }
-            if (y < wy) {
-              T* dst = fout + (size_t(z) * wy + y) * px + x0 + lane * V16;
+              if (y < wy) {
+                T* dst = fout + (size_t(z) * wy + y) * px + x0 + lane * V16;
+                if constexpr (RP) {
+                  T* rrow = resb + (size_t(rj) * TY + (y - y0)) * SW + lane * V16;
 #pragma unroll
-              for (int k2 = 0; k2 < NV; k2++)
-                if (x0 + k2 * 32 * V16 + lane * V16 < px) vec16_store(dst + k2 * 32 * V16, o + k2 * V16);
-            }
-          };
-          if constexpr (BOX) {
-            // rows yw-1 .. yw+RY of the three planes, three at a time
-            T bw[3][3][NV][WV];  // [plane][row % 3][vector][window]
-            auto bring = [&](int j) {  // row yw-1+j of every plane into bw[.][j % 3]
+                  for (int k2 = 0; k2 < NV; k2++) sts16_unordered(rrow + k2 * 32 * V16, o + k2 * V16);
+                  if (y - y0 < H || y - y0 >= TY - H) {
 #pragma unroll
-              for (int dz = 0; dz < 3; dz++) {
-                const RowRef rw = row_ref(pl[dz], yw - 1 + j);
-                T v[V];
-                load_vals(rw, v);
-                hwin(rw, v, bw[dz][j % 3]);
+                    for (int k2 = 0; k2 < NV; k2++)
+                      if (x0 + k2 * 32 * V16 + lane * V16 < px) vec16_store(dst + k2 * 32 * V16, o + k2 * V16);
+                  } else {
+                    if (lane == 0) vec16_store(dst, o);
+                    if (lane == 31 && x0 + (NV - 1) * 32 * V16 + 31 * V16 < px)
+                      vec16_store(dst + (NV - 1) * 32 * V16, o + (NV - 1) * V16);
+                  }
+                } else {
+#pragma unroll
+                  for (int k2 = 0; k2 < NV; k2++)
+                    if (x0 + k2 * 32 * V16 + lane * V16 < px) vec16_store(dst + k2 * 32 * V16, o + k2 * V16);
+                }
               }
             };
-            bring(0);
-            bring(1);
-            static_for<RY>([&](auto ryc) {
-              constexpr int ry = decltype(ryc)::value;
-              bring(ry + 2);
-              T o[V], c[V];
+            if constexpr (BOX) {
+              // rows yw-1 .. yw+RY of the three planes, three at a time
+              T bw[3][3][NV][WV];  // [plane][row % 3][vector][window]
+              auto bring = [&](int j) {  // row yw-1+j of every plane into bw[.][j % 3]
 #pragma unroll
-              for (int i = 0; i < V; i++) {
-                const int kk = i / V16, e = i % V16;
-                auto u = [&](int dz, int dy, int dx) -> T { return bw[dz + 1][(ry + 1 + dy) % 3][kk][H + e + dx]; };
-                o[i] = stencil_point<T, SHAPE, FAST>(u);
-                c[i] = bw[1][(ry + 1) % 3][kk][H + e];
-              }
-              finish(yw + ry, o, c);
-            });
+                for (int dz = 0; dz < 3; dz++) {
+                  const RowRef rw = row_ref(pl[dz], yw - 1 + j);
+                  T v[V];
+                  load_vals(rw, v);
+                  hwin(rw, v, bw[dz][j % 3]);
+                }
+              };
+              bring(0);
+              bring(1);
+              static_for<RY>([&](auto ryc) {
+                constexpr int ry = decltype(ryc)::value;
+                bring(ry + 2);
+                T o[V], c[V];
+#pragma unroll
+                for (int i = 0; i < V; i++) {
+                  const int kk = i / V16, e = i % V16;
+                  auto u = [&](int dz, int dy, int dx) -> T { return bw[dz + 1][(ry + 1 + dy) % 3][kk][H + e + dx]; };
+                  o[i] = stencil_point<T, SHAPE, FAST>(u);
+                  c[i] = bw[1][(ry + 1) % 3][kk][H + e];
+                }
+                finish(yw + ry, o, c);
+              });
+            } else {
+              constexpr int NC = 2 * H + 1;
+              T cr[NC][V];  // rolling rows of the centre plane: row yw-H+j in cr[j % NC]
+              static_for<2 * H>([&](auto jc) {
+                constexpr int j = decltype(jc)::value;
+                load_vals(row_ref(pl[H], yw - H + j), cr[j]);
+              });
+              static_for<RY>([&](auto ryc) {
+                constexpr int ry = decltype(ryc)::value;
+                const int y = yw + ry;
+                load_vals(row_ref(pl[H], y + H), cr[(ry + 2 * H) % NC]);
+                T cen[NV][WV];
+                hwin(row_ref(pl[H], y), cr[(ry + H) % NC], cen);
+                T nz[2 * H][V];  // row y of planes z-H..z-1 then z+1..z+H
+#pragma unroll
+                for (int d = 1; d <= H; d++) {
+                  load_vals(row_ref(pl[H - d], y), nz[H - d]);
+                  load_vals(row_ref(pl[H + d], y), nz[H + d - 1]);
+                }
+                T o[V], c[V];
+#pragma unroll
+                for (int i = 0; i < V; i++) {
+                  const int kk = i / V16, e = i % V16;
+                  auto u = [&](int dz, int dy, int dx) -> T {
+                    if (dz != 0) return nz[dz < 0 ? H + dz : H + dz - 1][i];
+                    if (dy != 0) return cr[(ry + H + dy) % NC][i];
+                    return cen[kk][H + e + dx];
+                  };
+                  o[i] = stencil_point<T, SHAPE, FAST>(u);
+                  c[i] = cen[kk][H + e];
+                }
+                finish(y, o, c);
+              });
+            }
+          };
+          if constexpr (Cf::RES) {
+            if (rj >= 0) do_plane(std::true_type{});
+            else do_plane(std::false_type{});
           } else {
-            constexpr int NC = 2 * H + 1;
-            T cr[NC][V];  // rolling rows of the centre plane: row yw-H+j in cr[j % NC]
-            static_for<2 * H>([&](auto jc) {
-              constexpr int j = decltype(jc)::value;
-              load_vals(row_ref(pl[H], yw - H + j), cr[j]);
-            });
-            static_for<RY>([&](auto ryc) {
-              constexpr int ry = decltype(ryc)::value;
-              const int y = yw + ry;
-              load_vals(row_ref(pl[H], y + H), cr[(ry + 2 * H) % NC]);
-              T cen[NV][WV];
-              hwin(row_ref(pl[H], y), cr[(ry + H) % NC], cen);
-              T nz[2 * H][V];  // row y of planes z-H..z-1 then z+1..z+H
-#pragma unroll
-              for (int d = 1; d <= H; d++) {
-                load_vals(row_ref(pl[H - d], y), nz[H - d]);
-                load_vals(row_ref(pl[H + d], y), nz[H + d - 1]);
-              }
-              T o[V], c[V];
-#pragma unroll
-              for (int i = 0; i < V; i++) {
-                const int kk = i / V16, e = i % V16;
-                auto u = [&](int dz, int dy, int dx) -> T {
-                  if (dz != 0) return nz[dz < 0 ? H + dz : H + dz - 1][i];
-                  if (dy != 0) return cr[(ry + H + dy) % NC][i];
-                  return cen[kk][H + e + dx];
-                };
-                o[i] = stencil_point<T, SHAPE, FAST>(u);
-                c[i] = cen[kk][H + e];
-              }
-              finish(y, o, c);
-            });
+            do_plane(std::false_type{});
           }
           // plane at position q-H is not read by later outputs
           __syncwarp();
@@ -422,6 +544,29 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil3d_kernel(const __grid_const
     if (it + 1 < p.steps && p.persistent) {
       fence_proxy_async_global();
       if (!gbar.sync()) ok = false;
+    }
+  }
+  if (Cf::RES && ok && rn > 0 && !producer) {
+    // the resident planes into the launch's output field (each lane reads
+    // what it stored; the barrier keeps these loads behind those stores)
+    __syncwarp();
+    asm volatile("" ::: "memory");
+    T* fo = static_cast<T*>(p.f[(p.t0 + p.steps) & 1]);
+    const int x0 = (rtile % p.gx) * SW, y0 = (rtile / p.gx) * TY;
+    for (int j = 0; j < rn; j++) {
+      for (int r = wid * RY; r < wid * RY + RY; r++) {
+        if (y0 + r >= wy) break;
+        const T* src = resb + (size_t(j) * TY + r) * SW + lane * V16;
+        T* dst = fo + (size_t(rz0 + j) * wy + y0 + r) * px + x0 + lane * V16;
+#pragma unroll
+        for (int k2 = 0; k2 < NV; k2++) {
+          if (x0 + k2 * 32 * V16 + lane * V16 < px) {
+            T v[V16];
+            vec16_load(src + k2 * 32 * V16, v);
+            vec16_store(dst + k2 * 32 * V16, v);
+          }
+        }
+      }
     }
   }
   if (!ok && producer && lane == 0) {

@@ -10,6 +10,77 @@ namespace perks {
 
 int encode_tiled_3d(CUtensorMap* map, bool f64, void* base, int wx, int wy, int h, int px, int box_x, int box_y);
 
+// Planes of CTA b's range that may stay resident: the segment (z-run of one
+// tile) with the most planes no other CTA reads, capped at kr. The kernel
+// makes the same choice.
+inline int resident_planes_of(long long total, int h, int grid, int b, int H, int kr) {
+  const long long c_lo = total * b / grid, c_hi = total * (b + 1) / grid;
+  if (c_hi <= c_lo) return 0;
+  const int nseg = int((c_hi - 1) / h - c_lo / h + 1);
+  int best = 0;
+  for (int k = 0; k < nseg; k++) {
+    const long long tb = c_lo / h + k;
+    const int zl = int(std::max(c_lo, tb * h) - tb * h), zh = int(std::min(c_hi, (tb + 1) * h) - tb * h);
+    best = std::max(best, std::min(kr, (zh - H) - (zl + H)));
+  }
+  return best;
+}
+
+// Resident plane tiles per CTA that fit next to the ring (persistent
+// launches that run more than one step), as opts.cache_rows asks: -1 as many
+// as fit, 0 none, n at most n.
+template <class Cf>
+int max_resident_planes(const perks_stencil_opts& o, const DeviceInfo& dev) {
+  if (o.kernel != PERKS_KERNEL_PERSISTENT || o.cache_rows == 0) return 0;
+  const long long avail = (long long)dev.smem_optin - (long long)Cf::res_offset;
+  int k = int(std::max<long long>(0, avail / (long long)Cf::res_plane_bytes));
+  if (o.cache_rows > 0) k = std::min(k, o.cache_rows);
+  return k;
+}
+
+// Largest height at which the persistent kernel keeps on chip every plane
+// of every CTA's z-runs except the H at each end (the 3D counterpart of the
+// reference's --small domain, stencil/3dstencil/j3d.driver.cpp:62-144). 0
+// when no plane fits next to the ring.
+template <class Cf>
+int min_domain_planes(const perks_stencil_opts& o, int wy, int wx, int* h_out) {
+  const DeviceInfo* dev = device_info();
+  if (!dev) return PERKS_ERR_NO_DEVICE;
+  *h_out = 0;
+  perks_stencil_opts op = o;
+  op.kernel = PERKS_KERNEL_PERSISTENT;
+  const int kmax = max_resident_planes<Cf>(op, *dev);
+  if (kmax == 0) return PERKS_OK;
+  const int ctas = o.ctas > 0 ? std::min(o.ctas, dev->sms) : dev->sms;
+  const long long tiles = (long long)((wx + Cf::SW - 1) / Cf::SW) * ((wy + Cf::TY - 1) / Cf::TY);
+  const int H = Cf::H;
+  auto fully_cached = [&](int h) {
+    const long long total = tiles * h;
+    const int grid = int(std::min<long long>(total, ctas));
+    for (int b = 0; b < grid; b++) {
+      const long long c_lo = total * b / grid, c_hi = total * (b + 1) / grid;
+      const int nseg = int((c_hi - 1) / h - c_lo / h + 1);
+      int eligible = 0;
+      for (int k = 0; k < nseg; k++) {
+        const long long tb = c_lo / h + k;
+        const int zl = int(std::max(c_lo, tb * h) - tb * h), zh = int(std::min(c_hi, (tb + 1) * h) - tb * h);
+        eligible += std::max(0, (zh - H) - (zl + H));
+      }
+      if (eligible > resident_planes_of(total, h, grid, b, H, kmax)) return false;
+    }
+    return true;
+  };
+  // beyond this height some CTA holds more than kmax + 2H planes of a run
+  const long long top = ctas * (long long)(kmax + 2 * H) / tiles + 2;
+  for (long long h = std::min<long long>(top, 1 << 20); h >= 1; h--) {
+    if (fully_cached(int(h))) {
+      *h_out = int(h);
+      return PERKS_OK;
+    }
+  }
+  return PERKS_OK;
+}
+
 // d_in / d_out are device buffers, or host buffers when host_io is set.
 template <class T, int SHAPE, bool FAST>
 int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h, int wy, int wx, int steps,
@@ -25,9 +96,20 @@ int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h
   const long long pairs = (long long)gx * gy * h;  // (tile, plane) pairs
   if (pairs > (1ll << 40)) return fail(PERKS_ERR_UNSUPPORTED, "3D domain too large");
   const int px = (wx + Cf::V16 - 1) / Cf::V16 * Cf::V16;
-  const size_t smem = Cf::smem_bytes;
-  if (smem > dev->smem_optin) return fail(PERKS_ERR_UNSUPPORTED, "shared memory budget exceeded");
+  if (Cf::smem_bytes > dev->smem_optin) return fail(PERKS_ERR_UNSUPPORTED, "shared memory budget exceeded");
   const int grid = int(std::min<long long>(pairs, ctas));
+  // resident planes: no more than the longest eligible run needs
+  int kr = 0;
+  long long cached = 0;
+  if (persistent && steps > 1) {
+    const int kmax = max_resident_planes<Cf>(o, *dev);
+    for (int b = 0; b < grid && kmax > 0; b++) {
+      const int n = resident_planes_of(pairs, h, grid, b, Cf::H, kmax);
+      kr = std::max(kr, n);
+      cached += n;
+    }
+  }
+  const size_t smem = kr > 0 ? Cf::res_offset + size_t(kr) * Cf::res_plane_bytes : Cf::smem_bytes;
   if (st) {
     *st = perks_stencil_stats{};
     st->grid_x = gx;
@@ -35,7 +117,7 @@ int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h
     st->grid_z = int((pairs + grid - 1) / grid);  // planes per CTA and step
     st->tile_x = Cf::SW;
     st->tile_y = Cf::TY;
-    st->cached_rows = 0;
+    st->cached_rows = kr;  // planes per CTA
   }
   const size_t elems = size_t(h) * wy * wx;
   if (steps == 0) {
@@ -62,7 +144,10 @@ int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h
       return stt;
     if ((stt = encode_tiled_3d(&p.pmap[i], sizeof(T) == 8, base, wx, wy, h, px, Cf::HP, Cf::SR)) != PERKS_OK)
       return stt;
+    if (kr > 0 && (stt = encode_tiled_3d(&p.hmap[i], sizeof(T) == 8, base, wx, wy, h, px, Cf::SW, Cf::H)) != PERKS_OK)
+      return stt;
   }
+  p.kr = kr;
   p.f[0] = f0;
   p.f[1] = f1;
   p.h = h;
@@ -78,7 +163,8 @@ int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h
   p.status = sw.status;
   p.ctl = wait_ctl();
 
-  auto kern = stencil3d_kernel<T, SHAPE, FAST, Cf>;
+  // the kernel built with resident planes only where one is kept
+  auto kern = kr > 0 ? stencil3d_kernel<T, SHAPE, FAST, Cfg3D<T, SHAPE, FAST, true>> : stencil3d_kernel<T, SHAPE, FAST, Cf>;
   PERKS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   cudaEvent_t e0, e1;
   PERKS_CUDA(cudaEventCreate(&e0));
@@ -131,7 +217,7 @@ int launch_stencil3d(const perks_stencil_opts& o, const T* d_in, T* d_out, int h
   if (st) {
     st->ms = ms;
     st->gcells_per_s = double(elems) * steps / (double(ms) * 1e6);
-    st->cached_fraction = 0.0;
+    st->cached_fraction = double(cached) / double(pairs);
     st->launches = launches;
   }
   return PERKS_OK;

@@ -30,7 +30,7 @@ def _stencil(a):
     g = torch.Generator(device="cpu").manual_seed(1)
     d = torch.rand(dims, generator=g, dtype=dt).cuda()
     o = torch.empty_like(d)
-    kw = dict(kernel=a.kernel, order=a.order, l2_sweep=a.l2_sweep)
+    kw = dict(kernel=a.kernel, order=a.order, l2_sweep=a.l2_sweep, cache_rows=a.cache_rows)
     fn = S.stencil2d if len(dims) == 2 else S.stencil3d
     fn(d, a.shape, 2, out=o, **kw)
     torch.cuda.synchronize()
@@ -138,6 +138,9 @@ def main(argv=None):
     s.add_argument("--kernel", default="persistent", choices=["persistent", "per_step", "naive"])
     s.add_argument("--l2-sweep", action="store_true")
     s.add_argument("--steps", type=int, default=3)
+    s.add_argument("--cache-rows", type=int, default=None,
+                   help="rows (2D) / planes (3D) per CTA kept in shared memory: -1 as many as fit, 0 none "
+                        "(default: the library's, 2D -1, 3D 0)")
     c = sub.add_parser("cg")
     c.add_argument("--matrix", default="lap2d", choices=["lap2d", "lap3d", "spd"])
     c.add_argument("--n", type=int, default=512, help="grid points per dimension (spd: rows)")

@@ -19,8 +19,10 @@ import numpy as np
 from . import _native as N
 
 
-def _opts(shape: str, dtype, order="reference", kernel="persistent", boundary="clamp", cache_rows=-1,
+def _opts(shape: str, dtype, order="reference", kernel="persistent", boundary="clamp", cache_rows=None,
           l2_sweep=False, ctas=0, stream=None, tma=False) -> N.StencilOpts:
+    """Options for one call; cache_rows None keeps the library's default
+    (2D: as many resident rows as fit; 3D: no resident planes)."""
     if shape not in N.SHAPES:
         raise ValueError(f"unknown shape {shape!r}")
     o = N.StencilOpts()
@@ -29,7 +31,8 @@ def _opts(shape: str, dtype, order="reference", kernel="persistent", boundary="c
     o.order = {"reference": N.ORDER_REFERENCE, "fast": N.ORDER_FAST}[order]
     o.kernel = {"persistent": N.KERNEL_PERSISTENT, "per_step": N.KERNEL_PER_STEP, "naive": N.KERNEL_NAIVE}[kernel]
     o.boundary = {"clamp": N.CLAMP, "dirichlet": N.DIRICHLET}[boundary]
-    o.cache_rows = int(cache_rows)
+    if cache_rows is not None:
+        o.cache_rows = int(cache_rows)
     o.l2_sweep = int(bool(l2_sweep))
     o.ctas = int(ctas)
     o.stream = stream
@@ -90,6 +93,17 @@ def min_domain_2d(shape: str, width_x: int, dtype=np.float32, **kw) -> int:
     wy = ctypes.c_int(0)
     N.check(N.lib().perks_stencil2d_min_domain(ctypes.byref(o), int(width_x), ctypes.byref(wy)))
     return wy.value
+
+
+def min_domain_3d(shape: str, width_y: int, width_x: int, dtype=np.float32, **kw) -> int:
+    """Largest height at which the persistent 3D kernel keeps every plane
+    tile that no other CTA reads on chip between steps (the reference's
+    getminHeight, stencil/3dstencil/j3d.driver.cpp:62-144); 0 when no plane
+    tile fits or the options cache nothing."""
+    o = _opts(shape, dtype, **kw)
+    h = ctypes.c_int(0)
+    N.check(N.lib().perks_stencil3d_min_domain(ctypes.byref(o), int(width_y), int(width_x), ctypes.byref(h)))
+    return h.value
 
 
 def getMinWidthY(width_x: int, bdimx: int = 256, registers: int = 0, useSM: bool = True, blkpsm: int = 0,

@@ -173,3 +173,15 @@ def test_division_check_rejects_unknown_divisor(native):
     assert L.perks_debug_div_check(7, 0, bad, None) == -10
     assert L.perks_debug_div_check(118, 2, bad, None) == -10
     assert L.perks_debug_div_check(118, 0, None, None) == -10
+
+
+def test_min_domain_3d_argument_errors(native):
+    L = native.lib()
+    N = native._native
+    o = N.StencilOpts()
+    L.perks_stencil_default_opts(ctypes.byref(o), 16, N.FP32)
+    h = ctypes.c_int(-1)
+    assert L.perks_stencil3d_min_domain(None, 8, 8, ctypes.byref(h)) == -10
+    assert L.perks_stencil3d_min_domain(ctypes.byref(o), 0, 8, ctypes.byref(h)) == -10
+    o.shape = 0
+    assert L.perks_stencil3d_min_domain(ctypes.byref(o), 8, 8, ctypes.byref(h)) == -10

@@ -51,9 +51,13 @@ def test_min_domain_without_cache(native, cuda):
     assert 0 < two < full and two % (2 + 2 * native.HALO["2d5pt"]) == 0
 
 
-def test_j3d_min_height_is_zero(native, cuda):
-    # the 3D kernel keeps no planes on chip: the reference's no-cache answer
-    assert native.j3d_iterative(None, 64, 64, 64, None, getminHeight=True, shape="3d7pt") == 0
+def test_j3d_min_height(native, cuda):
+    """getminHeight answers the 3D minimum-domain height (resident plane
+    tiles), and 0 without shared-memory caching (the reference's no-cache
+    answer)."""
+    h = native.j3d_iterative(None, 64, 64, 64, None, getminHeight=True, shape="3d7pt")
+    assert h > 0 and h == native.min_domain_3d("3d7pt", 64, 64, cache_rows=-1)
+    assert native.j3d_iterative(None, 64, 64, 64, None, getminHeight=True, useSM=False, shape="3d7pt") == 0
 
 
 def test_min_domain_rejects_too_wide(native, cuda):

@@ -49,6 +49,22 @@ def test_stencil_barrier_timeout(native, cuda, oracle, shape, dims, dt, skip_cta
     assert bits_equal(g, oracle.stencil(shape, f, 4))
 
 
+@pytest.mark.parametrize("shape", ["3d7pt", "3d27pt"])
+def test_stencil3d_resident_barrier_timeout(native, cuda, oracle, shape):
+    """With resident planes (few CTAs, long z-runs) the 3D kernel leaves
+    cleanly on a barrier timeout and writes none of its planes back."""
+    import torch
+    f = np.random.default_rng(9).random((40, 50, 70)).astype(np.float32)
+    t = torch.from_numpy(f).to(cuda)
+    with wait_fault(native, 1):
+        with pytest.raises(native.PerksError) as e:
+            native.stencil3d(t, shape, 4, kernel="persistent", ctas=3, cache_rows=-1)
+    assert e.value.code == TIMEOUT, str(e.value)
+    g, st = run(native, cuda, f, shape, 4, kernel="persistent", ctas=3, cache_rows=-1)
+    assert st["cached_rows"] > 0
+    assert bits_equal(g, oracle.stencil(shape, f, 4))
+
+
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
 def test_stencil_tma_barrier_timeout(native, cuda, oracle, dt):
     """The TMA-fed 2D kernel leaves cleanly when the grid barrier times out
