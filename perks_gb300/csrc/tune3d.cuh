@@ -15,8 +15,8 @@ struct Tune3D {
 // clang-format off
 // BEGIN TABLE
 constexpr Tune3D kTune3D[2][2][5] = {
-  {{{0, 0, 0}, {15, 4, 72}, {0, 0, 0}, {8, 4, 72}, {15, 4, 72}},
-   {{11, 4, 72}, {15, 4, 72}, {15, 4, 72}, {15, 4, 72}, {15, 4, 72}}},
+  {{{0, 0, 0}, {15, 4, 72}, {0, 0, 0}, {8, 4, 72}, {15, 4, 1}},
+   {{11, 4, 72}, {15, 4, 72}, {15, 4, 72}, {15, 4, 72}, {15, 4, 1}}},
   {{{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}},
    {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}}}};
 // END TABLE
