@@ -591,7 +591,8 @@ def extra_batch(P, torch, n_jobs=512, steps=100, seed=42):
                           "speedup_vs_plain_fp64": round(fp64_ms / st["ms"], 2),
                           "cg_worst_true_rel_res": worst, "threads": st["threads"],
                           "ctas_per_sm": st["ctas_per_sm"], "resident_stencil_jobs": st["resident_jobs"],
-                          "sliced_stencil_jobs": st["sliced_jobs"], "jobs_not_ok": bad}}
+                          "sliced_stencil_jobs": st["sliced_jobs"], "slicing": st["slicing"],
+                          "jobs_not_ok": bad}}
 
 
 def kernel_cached_fraction(P, d_in, d_out):

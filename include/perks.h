@@ -345,6 +345,9 @@ typedef struct {
   int threads;       /* threads per CTA (256, 512 or 1024); 0 = autotune */
   int ctas_per_sm;   /* 1 or 2; 0 = autotune */
   void* stream;      /* cudaStream_t; NULL = default stream */
+  int slicing;       /* work granularity: a stencil job costlier than (total cost) / (slicing x SMs)
+                        is cut into row slices run by several CTAs; 1, 2, 4, 8 or 16; 0 = autotune
+                        over 2..16 */
 } perks_batch_opts;
 
 typedef struct {
@@ -353,6 +356,7 @@ typedef struct {
   int resident_jobs;  /* stencil jobs kept in shared memory for all steps */
   int tuned;          /* 1 if the launch shape came from the autotuner */
   int sliced_jobs;    /* stencil jobs cut into row slices run by several CTAs */
+  int slicing;        /* the work granularity in use (see perks_batch_opts) */
 } perks_batch_stats;
 
 typedef struct perks_batch_plan_s* perks_batch_plan;

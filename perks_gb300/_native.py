@@ -76,12 +76,12 @@ class JobResult(ctypes.Structure):
 
 
 class BatchOpts(ctypes.Structure):
-    _fields_ = [("threads", c_int), ("ctas_per_sm", c_int), ("stream", c_void_p)]
+    _fields_ = [("threads", c_int), ("ctas_per_sm", c_int), ("stream", c_void_p), ("slicing", c_int)]
 
 
 class BatchStats(ctypes.Structure):
     _fields_ = [("ms", c_double), ("threads", c_int), ("ctas_per_sm", c_int), ("grid", c_int),
-                ("resident_jobs", c_int), ("tuned", c_int), ("sliced_jobs", c_int)]
+                ("resident_jobs", c_int), ("tuned", c_int), ("sliced_jobs", c_int), ("slicing", c_int)]
 
 
 JOB_STENCIL, JOB_CG = 0, 1

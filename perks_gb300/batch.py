@@ -49,7 +49,10 @@ def cg_job(row_ptr, col, val, b, x, tol: float = 1e-10, max_iter: int = 100000, 
 
 
 class BatchPlan:
-    def __init__(self, jobs: list[dict], threads: int = 0, ctas_per_sm: int = 0, stream=None):
+    def __init__(self, jobs: list[dict], threads: int = 0, ctas_per_sm: int = 0, stream=None, slicing: int = 0):
+        """threads, ctas_per_sm: the launch shape (0: autotuned); slicing: the
+        work granularity, a stencil job costlier than total / (slicing x SMs)
+        is cut into row slices (1, 2, 4, 8 or 16; 0: autotuned over 2..16)."""
         import torch
         self._jobs = jobs  # keeps the tensors alive
         arr = (N.Job * len(jobs))()
@@ -65,7 +68,7 @@ class BatchPlan:
                 J.d_b, J.d_x = j["b"].data_ptr(), j["x"].data_ptr()
         o = N.BatchOpts()
         N.lib().perks_batch_default_opts(ctypes.byref(o))
-        o.threads, o.ctas_per_sm = int(threads), int(ctas_per_sm)
+        o.threads, o.ctas_per_sm, o.slicing = int(threads), int(ctas_per_sm), int(slicing)
         o.stream = stream if stream is not None else torch.cuda.current_stream().cuda_stream
         self._plan = ctypes.c_void_p()
         N.check(N.lib().perks_batch_plan_create(arr, len(jobs), ctypes.byref(o), ctypes.byref(self._plan)))

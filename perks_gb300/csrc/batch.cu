@@ -409,7 +409,7 @@ struct perks_batch_plan_s {
   std::vector<long long> cells_of;  // per queue position, stencil cells x sizeof (0 for CG)
   BJob* d_jobs = nullptr;
   BItem* d_items = nullptr;
-  int nitems = 0, sliced = 0;
+  int nitems = 0, sliced = 0, slicing = 0;
   BRes* d_res = nullptr;
   unsigned* d_counter = nullptr;
   void* d_scratch = nullptr;
@@ -482,6 +482,8 @@ int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_
   if (o.threads != 0 && o.threads != 256 && o.threads != 512 && o.threads != 1024)
     return fail(PERKS_ERR_INVALID_ARG, "threads must be 0, 256, 512 or 1024");
   if (o.ctas_per_sm < 0 || o.ctas_per_sm > 2) return fail(PERKS_ERR_INVALID_ARG, "ctas_per_sm must be 0, 1 or 2");
+  if (o.slicing != 0 && o.slicing != 1 && o.slicing != 2 && o.slicing != 4 && o.slicing != 8 && o.slicing != 16)
+    return fail(PERKS_ERR_INVALID_ARG, "slicing must be 0, 1, 2, 4, 8 or 16");
   const DeviceInfo* dev = device_info();
   if (!dev) return PERKS_ERR_NO_DEVICE;
 
@@ -581,30 +583,45 @@ int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_
   if ((e = cudaMemcpy(p->d_jobs, table.data(), sizeof(BJob) * njobs, cudaMemcpyHostToDevice)) != cudaSuccess)
     return bail(cuda_fail(e, "cudaMemcpy(jobs)"));
 
-  // work items: stencil jobs above the balancing unit are cut into row slices
-  // (at most one per SM, so every slice of a job can be held at once)
+  // work items: stencil jobs above the balancing unit, total cost /
+  // (slicing x SMs), are cut into row slices (at most one per SM, so every
+  // slice of a job can be held at once)
   double total_cost = 0.0;
   for (int i = 0; i < njobs; i++) total_cost += cost[i];
-  const double unit = total_cost / (2.0 * dev->sms);
-  std::vector<BItem> items;
-  for (int q = 0; q < njobs; q++) {
-    const perks_job& J = jobs[p->order[q]];
-    int g = 1;
-    if (J.kind == PERKS_JOB_STENCIL && J.steps > 0) {
-      const int rows = J.h * J.wy;
-      g = int(std::min<double>(std::ceil(cost[p->order[q]] / unit), double(std::min(dev->sms, rows))));
-      g = std::max(g, 1);
+  auto build_items = [&](int slicing, int* sliced) {
+    const double unit = total_cost / (double(slicing) * dev->sms);
+    std::vector<BItem> items;
+    *sliced = 0;
+    for (int q = 0; q < njobs; q++) {
+      const perks_job& J = jobs[p->order[q]];
+      int g = 1;
+      if (J.kind == PERKS_JOB_STENCIL && J.steps > 0) {
+        const int rows = J.h * J.wy;
+        g = int(std::min<double>(std::ceil(cost[p->order[q]] / unit), double(std::min(dev->sms, rows))));
+        g = std::max(g, 1);
+      }
+      if (g > 1) ++*sliced;
+      const int rows = J.kind == PERKS_JOB_STENCIL ? J.h * J.wy : 0;
+      for (int sl = 0; sl < g; sl++)
+        items.push_back(BItem{q, sl, g, int((long long)rows * sl / g), int((long long)rows * (sl + 1) / g)});
     }
-    if (g > 1) p->sliced++;
-    const int rows = J.kind == PERKS_JOB_STENCIL ? J.h * J.wy : 0;
-    for (int sl = 0; sl < g; sl++)
-      items.push_back(BItem{q, sl, g, int((long long)rows * sl / g), int((long long)rows * (sl + 1) / g)});
+    return items;
+  };
+  // room for the finest granularity's items
+  size_t max_items = 0;
+  for (int f : {1, 2, 4, 8, 16}) {
+    int sl = 0;
+    max_items = std::max(max_items, build_items(f, &sl).size());
   }
-  p->nitems = int(items.size());
-  if ((e = cudaMalloc(&p->d_items, sizeof(BItem) * items.size())) != cudaSuccess)
+  if ((e = cudaMalloc(&p->d_items, sizeof(BItem) * max_items)) != cudaSuccess)
     return bail(cuda_fail(e, "cudaMalloc(items)"));
-  if ((e = cudaMemcpy(p->d_items, items.data(), sizeof(BItem) * items.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
-    return bail(cuda_fail(e, "cudaMemcpy(items)"));
+  auto use_items = [&](int slicing) -> cudaError_t {
+    const std::vector<BItem> items = build_items(slicing, &p->sliced);
+    p->nitems = int(items.size());
+    p->slicing = slicing;
+    return cudaMemcpy(p->d_items, items.data(), sizeof(BItem) * items.size(), cudaMemcpyHostToDevice);
+  };
+  if ((e = use_items(o.slicing ? o.slicing : 2)) != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy(items)"));
 
   // launch shape: the caller's, or the fastest candidate of one timed run each
   std::vector<std::pair<int, int>> cand;
@@ -650,13 +667,37 @@ int perks_batch_plan_create(const perks_job* jobs, int njobs, const perks_batch_
       }
     }
   }
-  p->tuned = cand.size() > 1;
+  // work granularity: the caller's, or (tuning) the fastest of 2, 4, 8 and 16
+  // at the chosen launch shape (1, measured twice as slow on the benchmark's
+  // workload, only when asked for)
+  if (o.slicing == 0) {
+    int best_f = p->slicing;
+    if (best == 0.f) {  // fixed launch shape: time the default granularity first
+      float ms = 0.f;
+      int rc = launch_once(p, p->stream, p->threads, p->ctas_per_sm, smem_for(dev, p->ctas_per_sm), &ms);
+      if (rc != PERKS_OK) return bail(rc);
+      best = ms;
+    }
+    for (int f : {4, 8, 16}) {
+      if ((e = use_items(f)) != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy(items)"));
+      float ms = 0.f;
+      int rc = launch_once(p, p->stream, p->threads, p->ctas_per_sm, smem_for(dev, p->ctas_per_sm), &ms);
+      if (rc != PERKS_OK) return bail(rc);
+      if (ms < best) {
+        best = ms;
+        best_f = f;
+      }
+    }
+    if ((e = use_items(best_f)) != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy(items)"));
+  }
+  p->tuned = cand.size() > 1 || o.slicing == 0;
   p->smem = smem_for(dev, p->ctas_per_sm);
   p->grid = dev->sms * p->ctas_per_sm;
   p->resident = 0;
   {
     std::vector<int> slices(njobs, 1);
-    for (const BItem& it : items) slices[it.job] = it.nslices;
+    int sl_count = 0;
+    for (const BItem& it : build_items(p->slicing, &sl_count)) slices[it.job] = it.nslices;
     for (int q = 0; q < njobs; q++)
       if (slices[q] == 1 && p->cells_of[q] > 0 && 2 * p->cells_of[q] <= (long long)p->smem) p->resident++;
   }
@@ -702,6 +743,7 @@ int perks_batch_plan_run(perks_batch_plan p, void* stream, perks_batch_stats* st
     st->resident_jobs = p->resident;
     st->tuned = p->tuned;
     st->sliced_jobs = p->sliced;
+    st->slicing = p->slicing;
   }
   return PERKS_OK;
 }

@@ -120,7 +120,7 @@ def _batch(a):
     import torch
     from .batch import BatchPlan, synthetic_workload
     jobs, _ = synthetic_workload(a.jobs, a.steps, a.seed)
-    with BatchPlan(jobs, threads=a.threads, ctas_per_sm=a.ctas) as plan:
+    with BatchPlan(jobs, threads=a.threads, ctas_per_sm=a.ctas, slicing=a.slicing) as plan:
         st = plan.run()
         bad = sum(1 for r in plan.results() if r["status"] != 0)
     torch.cuda.synchronize()
@@ -157,6 +157,7 @@ def main(argv=None):
     bt.add_argument("--seed", type=int, default=42)
     bt.add_argument("--threads", type=int, default=1024, help="threads per CTA (0 = autotune)")
     bt.add_argument("--ctas", type=int, default=1, help="CTAs per SM (0 = autotune)")
+    bt.add_argument("--slicing", type=int, default=2, help="work granularity 1, 2, 4, 8 or 16 (0 = autotune)")
     fp = sub.add_parser("fmapeak")
     fp.add_argument("--reps", type=int, default=5)
     a = ap.parse_args(argv)

@@ -54,20 +54,24 @@ def _build(cuda, torch, seed=7):
     return jobs, stencils, cgs
 
 
-@pytest.mark.parametrize("threads,ctas", [(0, 0), (256, 2), (1024, 1)])
-def test_batch_matches_oracle(native, cuda, oracle, threads, ctas):
+@pytest.mark.parametrize("threads,ctas,slicing", [(0, 0, 0), (256, 2, 1), (1024, 1, 4), (512, 1, 2), (1024, 1, 16),
+                                                   (1024, 1, 0)])
+def test_batch_matches_oracle(native, cuda, oracle, threads, ctas, slicing):
+    """Every launch shape and work granularity (slicing: stencil jobs costlier
+    than total / (slicing x SMs) are cut into row slices), tuned or fixed."""
     import torch
     from perks_gb300.batch import BatchPlan
     jobs, stencils, cgs = _build(cuda, torch)
-    with BatchPlan(jobs, threads=threads, ctas_per_sm=ctas) as plan:
+    with BatchPlan(jobs, threads=threads, ctas_per_sm=ctas, slicing=slicing) as plan:
         for rep in range(2):
             for _, _, _, _, o in stencils:
                 o.fill_(float("nan"))
             st = plan.run()
             res = plan.results()
             torch.cuda.synchronize()
-            assert st["resident_jobs"] > 0 and st["sliced_jobs"] > 0
-            assert st["tuned"] == (1 if threads == 0 else 0)
+            assert st["resident_jobs"] > 0 and (st["sliced_jobs"] > 0 or st["slicing"] == 1)
+            assert st["tuned"] == (1 if threads == 0 or slicing == 0 else 0)
+            assert st["slicing"] in (1, 2, 4, 8, 16) and (slicing == 0 or st["slicing"] == slicing)
             for j, shape, f, steps, o in stencils:
                 assert res[j]["status"] == 0 and res[j]["iterations"] == steps
                 assert bits_equal(o.cpu().numpy(), oracle.stencil(shape, f, steps)), (shape, f.shape, f.dtype, steps, rep)
