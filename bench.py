@@ -312,10 +312,16 @@ def main():
     kms = statistics.mean(kernel_ms)
     alg_bytes = 2 * 4 * cells  # reference formula: 2*sizeof(REAL)*cells per time step
     achieved = alg_bytes / (kms * 1e-3) / 1e9
+    traffic = (TRAFFIC_PER_CELL_STEP * cells) if TRAFFIC_PER_CELL_STEP else None
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_source": peak_src,
-            "traffic": (TRAFFIC_PER_CELL_STEP * cells) if TRAFFIC_PER_CELL_STEP else None,
+            "traffic": traffic,
             "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms_per_launch": round(kms, 3)}
+    if traffic:
+        # DRAM bytes actually moved (resident rows are not re-read) per second
+        dram = traffic / (kms * 1e-3) / 1e9
+        roof["dram_achieved"] = round(dram, 1)
+        roof["dram_frac"] = round(dram / peak, 4)
 
     extra = {}
     if not args.no_extra and rank == 0:
