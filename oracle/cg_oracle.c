@@ -3,7 +3,8 @@
  *
  * CPU restatement of the PERKS reference's conjugate-gradient iteration and
  * its SpMV, used by tests/, __graft_entry__.smoke() and bench.py's
- * cpu_baseline leg as the checker. The product library never links it.
+ * cpu_baseline leg to check or time against, never as the thing measured.
+ * The product library never links it.
  *
  * The iteration follows cpuConjugateGrad (conjugateGradient/cg_cpu.cpp:40-81)
  * step for step:

@@ -6,7 +6,7 @@ own CPU gold code (``_ref/libref_<shape>.so``, compiled unmodified from the
 reference sources by this directory's Makefile).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline import this
-module, and only as the checker.
+module, to check results against and to time the CPU path.
 """
 from __future__ import annotations
 

@@ -2,8 +2,8 @@
  * ORACLE — test infrastructure only.
  *
  * CPU restatement of the PERKS reference's CPU "gold" stencil code, used by
- * tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg as the
- * checker. Nothing in the product library links or calls this file.
+ * tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg to check
+ * or time against. Nothing in the product library links or calls this file.
  *
  * Parity pin: tests/test_oracle.py checks every shape and both precisions of
  * this file bit-for-bit against the reference's own gold functions compiled

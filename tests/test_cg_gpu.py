@@ -2,8 +2,8 @@
 restatement of the reference's CG, conjugateGradient/cg_cpu.cpp:40-81).
 
 CG on the GPU reduces dot products in a different order than the sequential
-CPU loop, so results are not bit-identical; the bar is the benchmark spec's:
-the same iteration count (within 1, or 1% for long solves) and a true
+CPU loop, so results are not bit-identical; the bar is the FP64 CG
+contract: the same iteration count (within 1, or 1% for long solves) and a true
 relative residual ||b - A x|| / ||b|| <= 1e-10 recomputed in FP64."""
 import numpy as np
 import pytest

@@ -126,7 +126,7 @@ def test_dirichlet_vs_oracle(native, cuda, oracle, shape, kernel):
 
 
 # Fast (FMA, folded coefficient) order. Tolerance: per-cell relative error
-# vs the FP64 reference-order oracle, 1e-12 for FP64 (the benchmark spec's bound),
+# vs the FP64 reference-order oracle, 1e-12 for FP64 (the plain FP64 path's per-cell bound),
 # 2e-5 for FP32 storage; shapes with positive weights only, so values stay
 # away from zero and the relative error is meaningful.
 @pytest.mark.parametrize("shape", ["2d5pt", "2ds9pt", "2ds25pt", "2d9pt", "2d25pt", "3d27pt", "3d17pt"])
