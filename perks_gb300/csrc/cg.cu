@@ -317,8 +317,16 @@ struct GridSum {
     return my_ok != 0;
   }
   __device__ bool bar() { return cl > 1 ? cluster_barrier() : gb.sync(); }
-  template <int NV>
-  __device__ bool sum_cluster(int slot, double (&v)[NV]) {
+  // `fin(totals)` runs on thread 0 of every CTA before the totals are
+  // broadcast: scalars derived from them (the CG quotients) are computed once
+  // per CTA and published in shared memory by the same barrier. A double
+  // division is a long FP64 sequence, and FP64 issue on this GPU is 2 lanes
+  // per clock per SM: all 1024 threads dividing would take microseconds.
+  struct NoFin {
+    __device__ void operator()(const double*) const {}
+  };
+  template <int NV, class Fin>
+  __device__ bool sum_cluster(int slot, double (&v)[NV], const Fin& fin) {
     __shared__ double cl_part[kMaxCluster][NV];
     __shared__ double cl_tot[NV];
     __shared__ unsigned cl_ok;
@@ -364,6 +372,7 @@ struct GridSum {
       my_ok = dsmem_ld_u32(dsmem_addr(&cl_ok, 0));
 #pragma unroll
       for (int k = 0; k < NV; k++) rs[k] = dsmem_ld_f64(dsmem_addr(&cl_tot[k], 0));
+      if (my_ok) fin(rs);
     }
     cluster_sync_all();  // the leader's results are read before they may change or the leader may leave
     if (my_ok == 0) return false;
@@ -371,10 +380,10 @@ struct GridSum {
     for (int k = 0; k < NV; k++) v[k] = rs[k];
     return true;
   }
-  template <int NV, bool WARP_DONE = false>
-  __device__ bool sum(int slot, double (&v)[NV]) {
+  template <int NV, bool WARP_DONE = false, class Fin = NoFin>
+  __device__ bool sum(int slot, double (&v)[NV], const Fin& fin = Fin{}) {
     block_sum_t0<NV, WARP_DONE>(v);
-    if (cl > 1) return sum_cluster<NV>(slot, v);
+    if (cl > 1) return sum_cluster<NV>(slot, v, fin);
     const int G = gridDim.x;
     double* ps = part + size_t(slot) * 2 * G;
     if (threadIdx.x == 0)
@@ -393,32 +402,36 @@ struct GridSum {
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (threadIdx.x == 0) rs[k] = acc;
       }
+      if (threadIdx.x == 0) fin(rs);
     }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < NV; k++) v[k] = rs[k];
     return true;
   }
-  __device__ bool sum2(int slot, double& a, double& b) {
+  template <class Fin = NoFin>
+  __device__ bool sum2(int slot, double& a, double& b, const Fin& fin = Fin{}) {
     double v[2] = {a, b};
-    if (!sum<2>(slot, v)) return false;
+    if (!sum<2>(slot, v, fin)) return false;
     a = v[0];
     b = v[1];
     return true;
   }
-  __device__ bool sum1(int slot, double& a) {
+  template <class Fin = NoFin>
+  __device__ bool sum1(int slot, double& a, const Fin& fin = Fin{}) {
     double v[1] = {a};
-    if (!sum<1>(slot, v)) return false;
+    if (!sum<1>(slot, v, fin)) return false;
     a = v[0];
     return true;
   }
   // An FP32 per-thread partial: summed across the warp in FP32 (FP64 issue
   // is 1/64 of FP32 here), then across warps and CTAs in FP64.
-  __device__ bool sum1f(int slot, float a, double& out) {
+  template <class Fin = NoFin>
+  __device__ bool sum1f(int slot, float a, double& out, const Fin& fin = Fin{}) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
     double v[1] = {double(a)};
-    if (!sum<1, true>(slot, v)) return false;
+    if (!sum<1, true>(slot, v, fin)) return false;
     out = v[0];
     return true;
   }
@@ -664,11 +677,15 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
   T r1, r0;
   double bb;
   int k;
+  // alpha and beta, divided once per CTA by thread 0 in the finishing step of
+  // the reduction that produces their denominator or numerator
+  __shared__ T s_alpha, s_beta;
   if (P.resume) {  // r and the last p were restored by the host
     R.load(row0, row1);
-    __syncthreads();
     r1 = T(P.rr0);
     r0 = T(P.rrp0);
+    if (tid == 0) s_beta = r1 / r0;
+    __syncthreads();
     bb = P.bb0;
     k = P.k0 + 1;
   } else {
@@ -708,7 +725,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
     if constexpr (FUSE) {
       // p = r (first) or beta p_old + r, formed where it is gathered
       if (k > 1) {
-        const T beta = r1 / r0;
+        const T beta = s_beta;
         const T* __restrict__ po = static_cast<const T*>(P.p[(k + 1) & 1]);
         auto pg = [&](int c) { return fma(beta, po[c], r[c]); };
         cg_rows_spmv<FMT, T>(A, val, pg, row0, row1, sr, [&](int i) {
@@ -748,7 +765,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
       }
     } else {
       if (k > 1) {
-        const T beta = r1 / r0;
+        const T beta = s_beta;
         cg_rows4(row0, row1, true, [&](int i) {
           T pv[4], rv[4];
           ld4(p + i, pv);
@@ -779,18 +796,20 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
       });
     }
     double pap;
+    T* const sa = &s_alpha;
+    auto fin_alpha = [r1, sa](const double* t) { *sa = r1 / T(t[0]); };
     if constexpr (FUSE) {
-      if (!gs.sum1f(1 + (k & 1), float(pap_t), pap)) return;
+      if (!gs.sum1f(1 + (k & 1), float(pap_t), pap, fin_alpha)) return;
     } else {
       pap = double(pap_t);
-      if (!gs.sum1(1 + (k & 1), pap)) return;
+      if (!gs.sum1(1 + (k & 1), pap, fin_alpha)) return;
     }
     const T dot = T(pap);
     if (!(dot > T(0)) || !isfinite(double(dot))) {
       if (tid == 0 && blockIdx.x == 0) atomicOr(P.status, kErrBreakdown);
       return;
     }
-    const T alpha = r1 / dot;
+    const T alpha = s_alpha;
     T rrn_t = T(0);
     cg_rows4(row0, row1, xvec, [&](int i) {
       T xv[4], pv[4], av[4], rv[4];
@@ -817,11 +836,13 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_persistent(const __grid_cons
       rrn_t = fma(rn, rn, rrn_t);
     });
     double rrn;
+    T* const sb = &s_beta;
+    auto fin_beta = [r1, sb](const double* t) { *sb = T(t[0]) / r1; };  // the next iteration's r1 / r0
     if constexpr (FUSE) {
-      if (!gs.sum1f(3, float(rrn_t), rrn)) return;
+      if (!gs.sum1f(3, float(rrn_t), rrn, fin_beta)) return;
     } else {
       rrn = double(rrn_t);
-      if (!gs.sum1(3, rrn)) return;
+      if (!gs.sum1(3, rrn, fin_beta)) return;
     }
     r0 = r1;
     r1 = T(rrn);
@@ -974,9 +995,19 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_single_red(const __grid_cons
     T g_t = T(0), d_t = T(0);
     spmv_w(g_t, d_t);
     double gn = double(g_t), dn = double(d_t);
-    if (!gs.sum2(1 + (k & 1), gn, dn)) return;
-    beta = gn / gamma_old;
-    const double den = dn - beta * gn / alpha;
+    // beta, the denominator and alpha, divided once per CTA by thread 0
+    __shared__ double s_q[3];
+    double* const q = s_q;
+    if (!gs.sum2(1 + (k & 1), gn, dn, [gamma_old, alpha, q](const double* t) {
+          const double bq = t[0] / gamma_old;
+          const double den_q = t[1] - bq * t[0] / alpha;
+          q[0] = bq;
+          q[1] = den_q;
+          q[2] = t[0] / den_q;
+        }))
+      return;
+    beta = s_q[0];
+    const double den = s_q[1];
     gamma_old = gn;
     gamma = gn;
     k++;
@@ -985,7 +1016,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_single_red(const __grid_cons
       if (tid == 0 && blockIdx.x == 0) atomicOr(P.status, kErrBreakdown);
       return;
     }
-    alpha = gn / den;
+    alpha = s_q[2];
   }
   X.store(row0, row1);
   if (blockIdx.x == 0 && tid == 0) {
@@ -1034,9 +1065,13 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
   };
   double rr, bb, maxrr, rr0;
   int k, outer, since;
+  // alpha and beta, divided once per CTA by thread 0 in the finishing step of
+  // the reduction that produces their denominator or numerator
+  __shared__ float s_alpha, s_beta;
   if (P.resume) {  // r, x_s and the last p restored by the host
     R.load(row0, row1);
     XS.load(row0, row1);
+    if (tid == 0) s_beta = float(P.rr0 / P.rrp0);
     __syncthreads();
     rr = P.rr0;
     rr0 = P.rrp0;
@@ -1074,7 +1109,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
     if constexpr (!FUSE) {
       // CSR / SELL: p in its own pass (same values as the fused form), so
       // that the SpMV gathers one vector instead of two
-      const float beta = k > 1 ? float(rr / rr0) : 0.0f;
+      const float beta = k > 1 ? s_beta : 0.0f;
       const float* __restrict__ po = static_cast<const float*>(P.p[(k + 1) & 1]);
       cg_rows4(row0, row1, true, [&](int i) {
         float pv[4], rv[4];
@@ -1097,7 +1132,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       });
     } else if (k > 1) {
       // formed where it is gathered (the values its owner stores are the same fma)
-      const float beta = float(rr / rr0);
+      const float beta = s_beta;
       const float* __restrict__ po = static_cast<const float*>(P.p[(k + 1) & 1]);
       auto pg = [&](int c) { return fmaf(beta, po[c], r[c]); };
       cg_rows_spmv<FMT, float>(A, val32, pg, row0, row1, sr, [&](int i) {
@@ -1136,12 +1171,13 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       });
     }
     double pap;
-    if (!gs.sum1f(1 + (k & 1), pap_t, pap)) return;
+    float* const sa = &s_alpha;
+    if (!gs.sum1f(1 + (k & 1), pap_t, pap, [rr, sa](const double* t) { *sa = float(rr / t[0]); })) return;
     if (!(pap > 0.0) || !isfinite(pap)) {
       if (tid == 0 && blockIdx.x == 0) atomicOr(P.status, kErrBreakdown);
       return;
     }
-    const float alpha = float(rr / pap);
+    const float alpha = s_alpha;
     float rrn_t = 0.0f;
     cg_rows4(row0, row1, true, [&](int i) {
       float xv[4], pv[4], av[4], rv[4];
@@ -1168,7 +1204,10 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
       rrn_t = fmaf(rn, rn, rrn_t);
     });
     double rrn;
-    if (!gs.sum1f(3, rrn_t, rrn)) return;
+    // the next iteration's rr / rr0 (replaced below after a reliable update)
+    float* const sb = &s_beta;
+    auto fin_beta = [rr, sb](const double* t) { *sb = float(t[0] / rr); };
+    if (!gs.sum1f(3, rrn_t, rrn, fin_beta)) return;
     since++;
     // the last allowed iteration folds x_s into x, unless a checkpoint takes
     // the state (then x_s is saved with it and the resumed solve continues
@@ -1189,7 +1228,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) cg_mixed(const __grid_constant_
         *R.at(i) = float(ri);
         rt = fma(ri, ri, rt);
       });
-      if (!gs.sum1(0, rt)) return;
+      if (!gs.sum1(0, rt, fin_beta)) return;
       rrn = rt;
       maxrr = rt;
       outer++;
