@@ -83,18 +83,35 @@ __device__ __forceinline__ bool job_barrier(unsigned* bar, unsigned target, long
   return s_ok != 0;
 }
 
-// CTA-wide sum of one double, valid in every thread (`red`: 32 doubles).
-__device__ __forceinline__ double cta_sum(double v, double* red) {
+// CTA-wide sum of one double, valid in every thread (`red`: kRed doubles).
+// Warp 0 adds the warp sums and thread 0 publishes the total, with `fin`
+// run on it: quotients derived from the total (alpha, beta) are divided once
+// per CTA and read from red[33..34] after the same barrier. FP64 issue is 2
+// lanes per clock per SM, so a second shuffle tree in every warp, or every
+// thread dividing, would cost microseconds per iteration.
+constexpr int kRed = 35;
+struct NoFin {
+  __device__ void operator()(double) const {}
+};
+template <class Fin = NoFin>
+__device__ __forceinline__ double cta_sum(double v, double* red, const Fin& fin = Fin{}) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   __syncthreads();
   if (lane == 0) red[w] = v;
   __syncthreads();
-  v = lane < nw ? red[lane] : 0.0;
+  if (w == 0) {
+    v = lane < nw ? red[lane] : 0.0;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) {
+      red[32] = v;
+      fin(v);
+    }
+  }
+  __syncthreads();
+  return red[32];
 }
 
 // One time step over rows [r_lo, r_hi) of the job's (h*wy) rows. L2 = true
@@ -217,12 +234,12 @@ __device__ void batch_cg(const BJob& J, double* red, BRes* res) {
       Ap[i] = acc;
       pap += double(p[i]) * double(acc);
     }
-    pap = cta_sum(pap, red);
+    pap = cta_sum(pap, red, [rr, red](double t) { red[33] = double(T(rr / t)); });
     if (!(pap > 0.0) || !isfinite(pap)) {
       status = PERKS_ERR_BREAKDOWN;
       break;
     }
-    const T alpha = T(rr / pap);
+    const T alpha = T(red[33]);
     double rrn = 0.0;
     for (int i = tid; i < n; i += nt) {
       x[i] = fma(alpha, p[i], x[i]);
@@ -230,8 +247,8 @@ __device__ void batch_cg(const BJob& J, double* red, BRes* res) {
       r[i] = ri;
       rrn += double(ri) * double(ri);
     }
-    rrn = cta_sum(rrn, red);
-    const T beta = T(rrn / rr);
+    rrn = cta_sum(rrn, red, [rr, red](double t) { red[34] = double(T(t / rr)); });
+    const T beta = T(red[34]);
     for (int i = tid; i < n; i += nt) p[i] = fma(beta, p[i], r[i]);
     rr = rrn;
     k++;
@@ -279,7 +296,7 @@ __device__ void batch_cg_mixed(const BJob& J, double* red, BRes* res) {
   double maxrr = rr, rr0 = 0.0;
   int k = 0, status = PERKS_OK;
   while (k < J.max_iter && rr > stop2) {
-    const float beta = k > 0 ? float(rr / rr0) : 0.0f;
+    const float beta = k > 0 ? float(red[34]) : 0.0f;  // rr / rr0, divided by thread 0 below
     for (int i = tid; i < n; i += nt) p[i] = k > 0 ? fmaf(beta, p[i], r[i]) : r[i];
     __syncthreads();  // p complete before the SpMV gathers it
     double pap = 0.0;
@@ -289,12 +306,12 @@ __device__ void batch_cg_mixed(const BJob& J, double* red, BRes* res) {
       Ap[i] = acc;
       pap += double(p[i] * acc);
     }
-    pap = cta_sum(pap, red);
+    pap = cta_sum(pap, red, [rr, red](double t) { red[33] = double(float(rr / t)); });
     if (!(pap > 0.0) || !isfinite(pap)) {
       status = PERKS_ERR_BREAKDOWN;
       break;
     }
-    const float alpha = float(rr / pap);
+    const float alpha = float(red[33]);
     double rrn = 0.0;
     for (int i = tid; i < n; i += nt) {
       xs[i] = fmaf(alpha, p[i], xs[i]);
@@ -302,7 +319,9 @@ __device__ void batch_cg_mixed(const BJob& J, double* red, BRes* res) {
       r[i] = ri;
       rrn += double(ri * ri);
     }
-    rrn = cta_sum(rrn, red);
+    // the next iteration's rr / rr0 (replaced after a reliable update)
+    auto fin_beta = [rr, red](double t) { red[34] = double(float(t / rr)); };
+    rrn = cta_sum(rrn, red, fin_beta);
     k++;
     if (rrn < 0.01 * maxrr || rrn <= stop2 || k == J.max_iter) {
       // reliable update: x += x_s in FP64, true residual with the FP64 values
@@ -319,7 +338,7 @@ __device__ void batch_cg_mixed(const BJob& J, double* red, BRes* res) {
         r[i] = float(ri);
         rt += ri * ri;
       }
-      rrn = cta_sum(rt, red);
+      rrn = cta_sum(rt, red, fin_beta);
       maxrr = rrn;
     }
     rr0 = rr;
@@ -339,7 +358,7 @@ __global__ void __launch_bounds__(1024, 1)
                  unsigned* counter, unsigned smem_bytes, const WaitCtl ctl) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int sq;
-  __shared__ double red[32];
+  __shared__ double red[kRed];
   while (true) {
     if (threadIdx.x == 0) sq = int(atomicAdd(counter, 1u));
     __syncthreads();
