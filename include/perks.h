@@ -414,8 +414,10 @@ PERKS_API int perks_debug_set_wait_fault(long long budget_cycles, int skip_cta);
 
 /* Check of the kernels' exact FP32 division by a constant (118: the 2D star
  * shapes; 159) over all 2^32 inputs against IEEE round-to-nearest division
- * on this GPU. `form` selects the finish (0 or 1, the 2D kernels' tuning
- * table picks one per shape). mismatches[2] receives the mismatch counts of
+ * on this GPU. `form` selects the finish (0 to 3, the 2D kernels' tuning
+ * table picks one per shape; 2 = the short path wherever its flag test is
+ * clear, the full finish elsewhere; 3 = the branch-free short finish).
+ * mismatches[2] receives the mismatch counts of
  * the two device forms (per element; packed pairs), first_bad[2] (may be
  * NULL) the lowest mismatching bit pattern of each (0xffffffff: none). */
 PERKS_API int perks_debug_div_check(int divisor, int form, long long* mismatches, unsigned* first_bad);

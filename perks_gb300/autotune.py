@@ -12,7 +12,8 @@ also the 16-byte vectors each lane holds per row (fewer cells per lane: a
 smaller register window, so more warps fit).
 
   1. compile every candidate of every translation unit of the kind with
-     -DPERKS_TUNE_* and -Xptxas -v, in parallel;
+     -DPERKS_TUNE_* and -Xptxas -v, in parallel (a 2D knob given as 0 keeps
+     each shape's table value, so one knob can be swept alone);
   2. record each kernel's spill bytes; a candidate that spills more than the
      built-in choice must win by a wider margin (5 % instead of 1 %);
   3. link one library per candidate and time every shape on the GPU
@@ -257,9 +258,13 @@ def read_table(path: str = TABLE, kind: str = "2d") -> dict:
 def merge_table(path: str, kind: str, table: dict) -> dict:
     """The header's table with the new winners written over it. Candidates
     are measured against the kernels the header already selects, so an entry
-    without a winner keeps its current value."""
+    without a winner keeps its current value, and a winner's knob of 0 (the
+    kernels then keep the table's value; the 2D division form has no such
+    value) keeps the entry's current one."""
     merged = read_table(path, kind)
-    merged.update({k: {n: v[n] for n, _ in KINDS[kind]["knobs"]} for k, v in table.items()})
+    for k, v in table.items():
+        old = merged.get(k, {})
+        merged[k] = {n: (v[n] if (v[n] or n == "fin") else old.get(n, 0)) for n, _ in KINDS[kind]["knobs"]}
     return merged
 
 
@@ -291,7 +296,7 @@ def main(argv=None) -> int:
     ap.add_argument("--orders", default="ref,fast")
     ap.add_argument("--nw", default="8,12,16,24", help="2D warps per CTA")
     ap.add_argument("--d", default="4,6", help="2D rows in flight per warp")
-    ap.add_argument("--fin", default="0,1", help="2D division form (reference order)")
+    ap.add_argument("--fin", default="0,1,2", help="2D division form (reference order)")
     ap.add_argument("--rp", default="1,2", help="2D rows per copy wait")
     ap.add_argument("--nv", default="0", help="2D 16-byte vectors per lane (0 = built-in)")
     ap.add_argument("--shapes", default="", help="only these shapes (comma-separated)")

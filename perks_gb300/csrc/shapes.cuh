@@ -95,8 +95,8 @@ __host__ __device__ constexpr double c27(int z, int y, int x) {
 // east, north, each term a rounded product added to the rounded running sum,
 // then / 118. `add(acc, p)` is the rounded sum (a packed-pair caller passes a
 // form ptxas cannot fuse with the product).
-template <class T, int SHAPE, int FIN = 0, class U, class Add>
-__device__ __forceinline__ T star2d_ref(const U& u, const Add& add) {
+template <class T, int SHAPE, class U, class Add>
+__device__ __forceinline__ T star2d_sum(const U& u, const Add& add) {
   using O = RN<T>;
   constexpr int H = ShapeInfo<SHAPE>::H;
   T acc = O::mul(T(star_s(H - 1)), u(0, -H, 0));
@@ -109,7 +109,11 @@ __device__ __forceinline__ T star2d_ref(const U& u, const Add& add) {
   for (int h = 0; h < H; h++) acc = add(acc, O::mul(T(star_e(h)), u(0, 0, 1 + h)));
 #pragma unroll
   for (int h = 0; h < H; h++) acc = add(acc, O::mul(T(star_n(h)), u(0, 1 + h, 0)));
-  return div_const<118, FIN>(acc);
+  return acc;
+}
+template <class T, int SHAPE, int FIN = 0, class U, class Add>
+__device__ __forceinline__ T star2d_ref(const U& u, const Add& add) {
+  return div_const<118, FIN>(star2d_sum<T, SHAPE>(u, add));
 }
 
 template <class T, int SHAPE, int FIN = 0, class U>

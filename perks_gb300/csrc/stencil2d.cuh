@@ -86,35 +86,31 @@ struct Geom2D {
 // Warps per CTA, rows in flight, division form, rows per copy wait and
 // vectors per lane for one kernel: the measured table (tune2d.cuh), else the
 // built-in choice. The tuning tool overrides them for a whole translation
-// unit with PERKS_TUNE_*.
+// unit with PERKS_TUNE_*; an override of 0 (for the division form: below 0)
+// keeps the table's value, so that one knob can be swept alone.
+#ifndef PERKS_TUNE_NV
+#define PERKS_TUNE_NV 0
+#endif
+#ifndef PERKS_TUNE_NW
+#define PERKS_TUNE_NW 0
+#endif
+#ifndef PERKS_TUNE_D
+#define PERKS_TUNE_D 0
+#endif
+#ifndef PERKS_TUNE_FIN
+#define PERKS_TUNE_FIN (-1)
+#endif
+#ifndef PERKS_TUNE_RP
+#define PERKS_TUNE_RP 0
+#endif
 template <class T, int SHAPE, bool FAST>
 struct Pick2D {
   static constexpr Tune2D t = kTune2D[sizeof(T) == 8][FAST][SHAPE];
-#ifdef PERKS_TUNE_NV
-  static constexpr int NVC = PERKS_TUNE_NV;
-#else
-  static constexpr int NVC = t.nv;  // 0 = built-in
-#endif
-#ifdef PERKS_TUNE_NW
-  static constexpr int NW = PERKS_TUNE_NW;
-#else
-  static constexpr int NW = t.nw ? t.nw : Geom2D<T, SHAPE, NVC>::NW_DEF;
-#endif
-#ifdef PERKS_TUNE_D
-  static constexpr int D = PERKS_TUNE_D;
-#else
-  static constexpr int D = t.d ? t.d : Geom2D<T, SHAPE, NVC>::d_def(NW);
-#endif
-#ifdef PERKS_TUNE_FIN
-  static constexpr int FIN = FAST ? 0 : PERKS_TUNE_FIN;
-#else
-  static constexpr int FIN = FAST ? 0 : t.fin;
-#endif
-#ifdef PERKS_TUNE_RP
-  static constexpr int RP = PERKS_TUNE_RP;
-#else
-  static constexpr int RP = t.rp ? t.rp : 1;
-#endif
+  static constexpr int NVC = PERKS_TUNE_NV ? PERKS_TUNE_NV : t.nv;  // 0 = built-in
+  static constexpr int NW = PERKS_TUNE_NW ? PERKS_TUNE_NW : t.nw ? t.nw : Geom2D<T, SHAPE, NVC>::NW_DEF;
+  static constexpr int D = PERKS_TUNE_D ? PERKS_TUNE_D : t.d ? t.d : Geom2D<T, SHAPE, NVC>::d_def(NW);
+  static constexpr int FIN = FAST ? 0 : PERKS_TUNE_FIN >= 0 ? PERKS_TUNE_FIN : t.fin;
+  static constexpr int RP = PERKS_TUNE_RP ? PERKS_TUNE_RP : t.rp ? t.rp : 1;
 };
 
 // Full configuration. The chosen values are template arguments, so kernels
@@ -474,7 +470,30 @@ __global__ void __launch_bounds__(Cf::NT, 1) stencil2d_kernel(const __grid_const
         WinT hc;  // star: horizontal window of the centre row
         if constexpr (!BOX) hc = hwin(w[ws(0)]);
         T o[V];
-        if constexpr (Cf::PAIR && !FAST) {
+        if constexpr (Cf::PAIR && !FAST && Cf::FIN == 2) {
+          // two adjacent cells per packed FP32 instruction; the division's
+          // finish only for a warp row with a subnormal midpoint or a
+          // non-finite value (divconst.cuh, FIN = 2)
+          F2 xs[V / 2], q[V / 2];
+          float e[V];
+#pragma unroll
+          for (int i = 0; i < V; i += 2) {
+            auto u2 = [&](int, int dy, int dx) -> F2 {
+              if (dy == 0) return F2::pack(hc.h[H + i + dx], hc.h[H + i + 1 + dx]);
+              return F2::pack(w[ws(dy)].v[i], w[ws(dy)].v[i + 1]);
+            };
+            xs[i / 2] = star2d_sum<F2, SHAPE>(u2, [one2](F2 a, F2 b) { return RN<F2>::fma(b, one2, a); });
+            F2 ep;
+            q[i / 2] = div_const_q1<118>(xs[i / 2], ep);
+            ep.unpack(e[i], e[i + 1]);
+          }
+          if (__any_sync(0xffffffffu, div_needs_finish<118>(e))) {
+#pragma unroll
+            for (int i = 0; i < V / 2; i++) q[i] = div_const<118, 1>(xs[i]);
+          }
+#pragma unroll
+          for (int i = 0; i < V; i += 2) q[i / 2].unpack(o[i], o[i + 1]);
+        } else if constexpr (Cf::PAIR && !FAST) {
           // two adjacent cells per packed FP32 instruction
 #pragma unroll
           for (int i = 0; i < V; i += 2) {

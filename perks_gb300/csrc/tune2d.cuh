@@ -15,7 +15,7 @@ struct Tune2D {
 // clang-format off
 // BEGIN TABLE
 constexpr Tune2D kTune2D[2][2][8] = {
-  {{{16, 4, 1, 0, 0}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {8, 6, 0, 1, 1}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}},
+  {{{16, 4, 1, 0, 0}, {0, 0, 3, 0, 0}, {0, 0, 3, 0, 0}, {0, 0, 3, 0, 0}, {0, 0, 2, 0, 0}, {8, 6, 3, 1, 1}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}},
    {{8, 4, 0, 0, 0}, {8, 6, 0, 0, 0}, {12, 6, 0, 2, 0}, {12, 6, 0, 0, 0}, {12, 4, 0, 0, 0}, {16, 6, 0, 1, 1}, {8, 4, 0, 0, 0}, {12, 4, 0, 0, 0}}},
   {{{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {8, 4, 1, 0, 0}, {12, 6, 0, 0, 0}, {12, 4, 0, 1, 0}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}},
    {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {12, 4, 0, 1, 0}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}}}};

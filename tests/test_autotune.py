@@ -68,6 +68,15 @@ def test_merge_keeps_entries_without_a_winner(tmp_path):
     assert m["f64/ref/2d21pt"] == {"nw": 12, "d": 6, "fin": 0, "rp": 0, "nv": 0}
 
 
+def test_merge_keeps_the_table_value_of_a_knob_swept_as_zero(tmp_path):
+    dst = tmp_path / "tune2d.cuh"
+    shutil.copy(A.TABLE, dst)
+    A.write_table({"f32/ref/2d5pt": {"nw": 16, "d": 4, "fin": 1, "rp": 2, "nv": 1}}, str(dst))
+    # only the division form was swept; the other knobs ran at their table values
+    m = A.merge_table(str(dst), "2d", {"f32/ref/2d5pt": {"nw": 0, "d": 0, "fin": 0, "rp": 0, "nv": 0, "gcells": 1.0}})
+    assert m["f32/ref/2d5pt"] == {"nw": 16, "d": 4, "fin": 0, "rp": 2, "nv": 1}
+
+
 def test_3d_table_roundtrip(tmp_path):
     dst = tmp_path / "tune3d.cuh"
     shutil.copy(A.KINDS["3d"]["table"], dst)

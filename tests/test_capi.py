@@ -171,7 +171,7 @@ def test_division_check_rejects_unknown_divisor(native):
     L = native.lib()
     bad = (ctypes.c_longlong * 2)()
     assert L.perks_debug_div_check(7, 0, bad, None) == -10
-    assert L.perks_debug_div_check(118, 2, bad, None) == -10
+    assert L.perks_debug_div_check(118, 4, bad, None) == -10
     assert L.perks_debug_div_check(118, 0, None, None) == -10
 
 
