@@ -135,7 +135,8 @@ __device__ __forceinline__ void stencil_rows(const BJob& J, const T* __restrict_
         if constexpr (L2) return __ldcg(a);
         else return *a;
       };
-      dst[((size_t)z * wy + y) * wx + x] = stencil_point<T, SHAPE, false>(u);
+      // FP32: the branch-free short finish of the exact division (divconst.cuh, form 3)
+      dst[((size_t)z * wy + y) * wx + x] = stencil_point<T, SHAPE, false, sizeof(T) == 4 ? 3 : 0>(u);
     }
   }
 }

@@ -116,6 +116,41 @@ __device__ __forceinline__ T star2d_ref(const U& u, const Add& add) {
   return div_const<118, FIN>(star2d_sum<T, SHAPE>(u, add));
 }
 
+// 3D stars, reference order: e, w, n, s, t, b (3d13pt: each side near then
+// far), every product and sum rounded, then minus the rounded centre term;
+// float-literal coefficients. `add(acc, p)` / `sub(acc, p)` are the rounded
+// sum and difference (a packed-pair caller passes forms ptxas cannot fuse
+// with the product).
+template <class T, int SHAPE, class U, class Add, class Sub>
+__device__ __forceinline__ T star3d_ref(const U& u, const Add& add, const Sub& sub) {
+  using O = RN<T>;
+  if constexpr (SHAPE == PERKS_3D7PT) {
+    T acc = O::mul(T(0.161f), u(0, 0, 1));
+    acc = add(acc, O::mul(T(0.162f), u(0, 0, -1)));
+    acc = add(acc, O::mul(T(0.163f), u(0, 1, 0)));
+    acc = add(acc, O::mul(T(0.164f), u(0, -1, 0)));
+    acc = add(acc, O::mul(T(0.165f), u(1, 0, 0)));
+    acc = add(acc, O::mul(T(0.166f), u(-1, 0, 0)));
+    return sub(acc, O::mul(T(1.67f), u(0, 0, 0)));
+  } else {
+    static_assert(SHAPE == PERKS_3D13PT, "3D star");
+    const T c = T(0.083f);
+    T acc = O::mul(c, u(0, 0, 1));
+    acc = add(acc, O::mul(c, u(0, 0, 2)));
+    acc = add(acc, O::mul(c, u(0, 0, -1)));
+    acc = add(acc, O::mul(c, u(0, 0, -2)));
+    acc = add(acc, O::mul(c, u(0, 1, 0)));
+    acc = add(acc, O::mul(c, u(0, 2, 0)));
+    acc = add(acc, O::mul(c, u(0, -1, 0)));
+    acc = add(acc, O::mul(c, u(0, -2, 0)));
+    acc = add(acc, O::mul(c, u(1, 0, 0)));
+    acc = add(acc, O::mul(c, u(2, 0, 0)));
+    acc = add(acc, O::mul(c, u(-1, 0, 0)));
+    acc = add(acc, O::mul(c, u(-2, 0, 0)));
+    return sub(acc, O::mul(T(0.996f), u(0, 0, 0)));
+  }
+}
+
 template <class T, int SHAPE, int FIN = 0, class U>
 __device__ __forceinline__ T point_ref(const U& u) {
   using O = RN<T>;
@@ -145,30 +180,8 @@ __device__ __forceinline__ T point_ref(const U& u) {
       }
     }
     return T(div_const<118, FIN>(accd));
-  } else if constexpr (SHAPE == PERKS_3D7PT) {
-    // e, w, n, s, t, b then minus the centre; float-literal coefficients.
-    T acc = O::mul(T(0.161f), u(0, 0, 1));
-    acc = O::add(acc, O::mul(T(0.162f), u(0, 0, -1)));
-    acc = O::add(acc, O::mul(T(0.163f), u(0, 1, 0)));
-    acc = O::add(acc, O::mul(T(0.164f), u(0, -1, 0)));
-    acc = O::add(acc, O::mul(T(0.165f), u(1, 0, 0)));
-    acc = O::add(acc, O::mul(T(0.166f), u(-1, 0, 0)));
-    return O::sub(acc, O::mul(T(1.67f), u(0, 0, 0)));
-  } else if constexpr (SHAPE == PERKS_3D13PT) {
-    const T c = T(0.083f);
-    T acc = O::mul(c, u(0, 0, 1));
-    acc = O::add(acc, O::mul(c, u(0, 0, 2)));
-    acc = O::add(acc, O::mul(c, u(0, 0, -1)));
-    acc = O::add(acc, O::mul(c, u(0, 0, -2)));
-    acc = O::add(acc, O::mul(c, u(0, 1, 0)));
-    acc = O::add(acc, O::mul(c, u(0, 2, 0)));
-    acc = O::add(acc, O::mul(c, u(0, -1, 0)));
-    acc = O::add(acc, O::mul(c, u(0, -2, 0)));
-    acc = O::add(acc, O::mul(c, u(1, 0, 0)));
-    acc = O::add(acc, O::mul(c, u(2, 0, 0)));
-    acc = O::add(acc, O::mul(c, u(-1, 0, 0)));
-    acc = O::add(acc, O::mul(c, u(-2, 0, 0)));
-    return O::sub(acc, O::mul(T(0.996f), u(0, 0, 0)));
+  } else if constexpr (SHAPE == PERKS_3D7PT || SHAPE == PERKS_3D13PT) {
+    return star3d_ref<T, SHAPE>(u, [](T a, T b) { return O::add(a, b); }, [](T a, T b) { return O::sub(a, b); });
   } else if constexpr (SHAPE == PERKS_3D17PT) {
     using D = RN<double>;
     T cb = O::add(u(-1, -1, -1), u(-1, -1, 1));
