@@ -166,12 +166,14 @@ def test_large_field_properties(native, cuda, oracle):
     assert bits_equal(a[y0:y0 + n, x0:x0 + n].cpu().numpy(), ref)
 
 
-@pytest.mark.parametrize("shape", ["2d5pt", "2ds9pt", "2d9pt", "2d25pt", "3d17pt", "3d27pt", "3d7pt"])
+@pytest.mark.parametrize("shape", ["2d5pt", "2ds9pt", "2d13pt", "2d21pt", "2ds25pt", "2d9pt", "2d25pt", "3d17pt",
+                                   "3d27pt", "3d7pt"])
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
 def test_extreme_values_bit_exact(native, cuda, oracle, shape, dt):
     """Subnormal, tiny, huge, infinite and NaN inputs: exercises the exact
-    constant-division paths (integer path for subnormal quotients, corrected
-    reciprocal otherwise) against the reference order on the CPU."""
+    constant-division paths against the reference order on the CPU, in
+    every finish form the FP32 star shapes use (2d5pt full, 2d21pt the
+    warp-vote short path, the others the branch-free short finish)."""
     rng = np.random.default_rng(21)
     dims = (64, 200) if shape.startswith("2d") else (12, 20, 70)
     tiny = np.finfo(dt).smallest_subnormal
