@@ -83,3 +83,20 @@ def test_3d_table_roundtrip(tmp_path):
     A.write_table({"f64/fast/poisson": {"nwc": 8, "ry": 2, "dkb": 96}}, str(dst), "3d")
     assert A.read_table(str(dst), "3d") == {"f64/fast/poisson": {"nwc": 8, "ry": 2, "dkb": 96}}
     assert A.parse_variant("s3d_f64_fast_nwc8_ry2_dkb96") == {"nwc": 8, "ry": 2, "dkb": 96}
+
+
+def test_committed_tables_are_in_range():
+    """Every entry of the committed tables names a setting the kernels build:
+    a value outside these ranges (say a division form of 4) would compile to
+    some other form without an error."""
+    for key, e in A.read_table(A.TABLE, "2d").items():
+        assert e["nw"] == 0 or 1 <= e["nw"] <= 32, (key, e)
+        assert e["d"] == 0 or 1 <= e["d"] <= 8, (key, e)
+        assert 0 <= e["fin"] <= 3, (key, e)
+        assert e["rp"] in (0, 1, 2), (key, e)
+        assert 0 <= e["nv"] <= 3, (key, e)
+        if "/fast/" in key:
+            assert e["fin"] == 0, key  # fast order has no division
+    for key, e in A.read_table(A.KINDS["3d"]["table"], "3d").items():
+        assert e["nwc"] == 0 or 1 <= e["nwc"] <= 31, (key, e)
+        assert e["ry"] >= 0 and e["dkb"] >= 0, (key, e)
